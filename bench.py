@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""Throughput of the fused XPFC step on GB300: grid-point-steps/s.
+
+Workload (one "step" = one semi-implicit time step of the whole field):
+256^3 periodic grid, dx = 0.125 (L = 32), two-peak fcc correlation kernel
+(k = 2 pi, 4 pi/sqrt 3; alpha = 1, 1; rho = 1, 1; beta = 8, 6; max envelope),
+eta = 2, chi = 1, n0 = 0.04, initial n = n0 + N(0, 0.05^2) (seeded Philox),
+conserved noise of amplitude 0.01 every step, dt = 1, diagnostics every 100
+steps; FP32 bulk with FP64 k = 0 and sums.  sigma = 0.22: at sigma = 0.12 this
+parameter set diverges under the reference's own scheme within 20 steps (the
+explicit nonlinear term), while the work per step does not depend on sigma.
+All inputs are synthetic and seeded.
+
+Default arm: libxpfc through its C ABI on one GPU per rank (replicas: every
+rank advances its own independent solve; no collective on the data path).
+--impl reference: the CPU implementation of the same step (the FP64 oracle
+restating the reference's loop, OpenMP on the host cores), rank 0 only.
+
+Prints one JSON line on rank 0.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "Gpt-steps/s @256^3 mixed vs FP64 on 1 GB300 (F rel<=1e-6); sweep solves/s, p99"
+UNIT = "Gpt-steps/s"
+DX = 0.125
+FCC = ((2 * math.pi, 1.0, 1.0, 8.0), (2 * math.pi * 2 / math.sqrt(3), 1.0, 1.0, 6.0))
+# per-pass algorithmic bytes as multiples of one packed field array (N^3 elements)
+PASS_NAMES = {0: "pencil_kernel", 1: "col_kernel(inverse)", 2: "row_kernel(fused)", 3: "col_kernel(forward)"}
+PASS_ARRAYS = {0: 3, 1: 2, 2: 2, 3: 2}
+SURVEY_BYTES_PER_POINT = 16.125   # two read+write sweeps of the FP32 state at 256^3
+SIGMA = 0.22
+
+
+def workload_params(X, n, precision, rank):
+    L = n * DX
+    return X.default_params(Mx=n, My=n, Mz=n, Lx=L, Ly=L, Lz=L, psi0=0.04, sigma=SIGMA, peaks=FCC,
+                            envelope=X._lib.ENVELOPE_MAX, a=1.0, b=1.0 / 3.0, eps=0.0, Mo=1.0, dt=1.0,
+                            nsteps=2001, t_sample=100, precision=precision, ic_kind=X._lib.IC_NOISE,
+                            ic_amp=0.05, ic_seed=1 + rank, noise_amp=0.01, noise_seed=11 + rank,
+                            ff_factor=DX ** 3, ref_compat=0)
+
+
+def config(n, precision):
+    return {"workload": "XPFC step %d^3, fcc kernel, conserved noise 0.01/step, %s" % (
+        n, "FP32 bulk + FP64 k=0 and sums" if precision == "mixed" else "FP64"),
+        "grid": n, "dx": DX, "sigma": SIGMA, "precision": precision, "diag_every": 100,
+        "l2": "flushed between timed steps (256 MB write outside the timed events)",
+        "parallelism": "replicas (one independent solve per GPU)"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(dev)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax = float(c[2])
+                power.append(float(c[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, c[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        load = [v for v in sm if smax and v > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline(n, steps=None, target_s=15.0):
+    """The FP64 oracle on the host cores over a bounded sample of the workload."""
+    import numpy as np  # noqa: F401
+    from oracle import oracle as O
+    L = n * DX
+    p = O.make_params(n, n, n, L=(L, L, L), a=1.0, b=1.0 / 3.0, sigma=SIGMA, peaks=FCC, envelope=1,
+                      ff_factor=DX ** 3, noise_amp=0.01, noise_seed=11)
+    psi = O.ic_noise(n, n, n, 0.04, 0.05, 1)
+    O.pin_mean(psi, 0.04)
+    if steps is None:
+        t1, _ = O.bench(p, psi, 1)
+        steps = max(1, min(40, int(target_s / max(t1, 1e-3))))
+    sec, _ = O.bench(p, psi, steps)
+    return {"value": n ** 3 * steps / sec / 1e9, "unit": UNIT, "cores": O.threads(), "kind": "port",
+            "sample": "%d full steps of the %d^3 workload (FP64 oracle, OpenMP, %d threads), %.1f s" % (
+                steps, n, O.threads(), sec)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    n = args.size
+    L = n * DX
+    p = O.make_params(n, n, n, L=(L, L, L), a=1.0, b=1.0 / 3.0, sigma=SIGMA, peaks=FCC, envelope=1,
+                      ff_factor=DX ** 3, noise_amp=0.01, noise_seed=11)
+    psi = O.ic_noise(n, n, n, 0.04, 0.05, 1)
+    O.pin_mean(psi, 0.04)
+    _, psi = O.bench(p, psi, args.warmup)
+    sec, _ = O.bench(p, psi, args.steps)
+    v = n ** 3 * args.steps / sec / 1e9
+    cb = {"value": v, "unit": UNIT, "cores": O.threads(), "kind": "port",
+          "sample": "%d timed steps (+%d warm-up) of the %d^3 workload, FP64 oracle restating the reference "
+                    "loop (main.cu:306-435); the reference itself is CUDA-only" % (args.steps, args.warmup, n)}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, "mixed"),
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_traffic(kernel, n):
+    """DRAM bytes per launch from the committed ncu summary, or None."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        e = t[kernel]
+        return e["bytes_per_launch_at"][str(n)]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def run_ours(args):
+    import torch
+    import numpy as np
+
+    import xpfc_cuda_gb300 as X
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist = None
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def allmax(v):
+        if not dist:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    n = args.size
+    prec = X._lib.MIXED if args.precision == "mixed" else X._lib.FP64
+    p = workload_params(X, n, prec, rank)
+    p.device = local
+    # a dedicated stream: the legacy default stream has handle 0, which the
+    # library would read as "make your own stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    host_psi = X.build_initial_field(p)
+    x = X.Xpfc(p, stream=stream.cuda_stream)
+    x.initialize(host_psi)
+    x.step_async(args.warmup)
+    x.collect()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    x.set_profiling(True)
+    launches0 = x.launch_count
+    barrier()
+    clk = Clocks(local)
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        x.step_async(1)
+        ends[k].record(stream)
+    x.collect()
+    barrier()
+    clocks = clk.stop()
+    launches = x.launch_count - launches0
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    prof = x.profile()
+    x.set_profiling(False)
+    ms_max = allmax(ms)
+    value = ws * n ** 3 * args.steps / (ms_max / 1e3) / 1e9
+
+    # FP64 plain path on the same workload (the "vs FP64" half of the metric)
+    fp64 = None
+    if not args.no_fp64 and args.precision == "mixed":
+        p64 = workload_params(X, n, X._lib.FP64, rank)
+        p64.device = local
+        with X.Xpfc(p64, stream=stream.cuda_stream) as y:
+            y.initialize(host_psi)
+            y.step_async(2)
+            y.collect()
+            k64 = max(3, args.steps // 4)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            barrier()
+            e0.record(stream)
+            y.step_async(k64)
+            e1.record(stream)
+            y.collect()
+            barrier()
+            t64 = allmax(e0.elapsed_time(e1))
+        fp64 = {"value": ws * n ** 3 * k64 / (t64 / 1e3) / 1e9, "unit": UNIT, "ms_per_step": t64 / k64,
+                "steps": k64, "l2": "not flushed (state 2 x 134 MB > L2)"}
+
+    # end to end through the C ABI with host buffers: upload the initial
+    # field, run the solve segment with its diagnostics, download the field
+    e2e = None
+    if not args.no_e2e:
+        ke = args.e2e_steps
+        out = np.empty(n ** 3)
+        barrier()
+        t0 = time.perf_counter()
+        x.initialize(host_psi)
+        recs = x.step(ke)
+        out[:] = x.copy2cpu().reshape(-1)
+        torch.cuda.synchronize()
+        te = allmax(time.perf_counter() - t0)
+        diag_bytes = 8 * 8 * max(1, len(recs))
+        e2e = {"value": ws * n ** 3 * ke / te / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(8 * n ** 3 / ke),
+               "d2h_bytes_per_step": int((4 * n ** 3 if prec == X._lib.MIXED else 8 * n ** 3) / ke + diag_bytes / ke),
+               "steps": ke, "seconds": te,
+               "what": "xpfc_initialize(host FP64 field) + xpfc_step(%d, diagnostics every 100) + "
+                       "xpfc_get_field(host)" % ke}
+
+    # roofline of the dominant pass
+    peak, peak_kind = measured_peak()
+    esz = 4 if prec == X._lib.MIXED else 8
+    passes = {k: v for k, v in prof.items() if k in PASS_NAMES and v[1] > 0}
+    dom = max(passes, key=lambda k: passes[k][0]) if passes else None
+    roof = None
+    if dom is not None:
+        avg_ms = passes[dom][0] / passes[dom][1]
+        alg = PASS_ARRAYS[dom] * esz * n ** 3
+        achieved = alg / (avg_ms / 1e3) / 1e9
+        traffic = load_traffic(PASS_NAMES[dom], n)
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": PASS_NAMES[dom], "algorithmic_bytes": alg,
+                "avg_launch_ms": avg_ms, "peak_source": peak_kind,
+                "passes": {PASS_NAMES[k]: {"avg_ms": v[0] / v[1], "launches": v[1],
+                                           "GB/s": PASS_ARRAYS[k] * esz * n ** 3 / (v[0] / v[1] / 1e3) / 1e9}
+                           for k, v in passes.items()},
+                "step_frac_of_two_sweep_floor": (value * 1e9 / ws) * SURVEY_BYTES_PER_POINT / (peak * 1e9)}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(n)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == X._lib.MIXED else "f64",
+                "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, args.precision),
+                "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+                "fp64": fp64}
+        print(json.dumps(line), flush=True)
+    x.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="xpfc", choices=["xpfc", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=2000)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

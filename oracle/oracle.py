@@ -62,6 +62,9 @@ def lib():
         L.ox_noise_k.argtypes = [C.POINTER(OxParams), C.c_long, dp]
         L.ox_run.argtypes = [C.POINTER(OxParams), dp, C.c_long, C.c_int, C.POINTER(OxDiag)]
         L.ox_run.restype = C.c_int
+        L.ox_bench.argtypes = [C.POINTER(OxParams), dp, C.c_long, dp]
+        L.ox_bench.restype = C.c_int
+        L.ox_threads.restype = C.c_int
         L.ox_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.ox_gauss_pair.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, dp, dp]
         L.ox_ic_noise.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64]
@@ -129,6 +132,19 @@ def run(p, psi, nsteps, t_sample):
     mean = np.array([d.mean for d in diag])
     rms = np.array([d.rms for d in diag])
     return psi, F, mean, rms
+
+
+def bench(p, psi, nsteps):
+    """Wall-clock seconds of nsteps oracle steps (no diagnostics)."""
+    psi = np.ascontiguousarray(psi, dtype=np.float64).copy()
+    sec = C.c_double()
+    if lib().ox_bench(C.byref(p), _dp(psi.reshape(-1)), nsteps, C.byref(sec)) != 0:
+        raise RuntimeError("ox_bench failed")
+    return sec.value, psi
+
+
+def threads():
+    return lib().ox_threads()
 
 
 def ic_noise(nx, ny, nz, n0, amp, seed):

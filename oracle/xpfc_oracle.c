@@ -509,6 +509,7 @@ void ox_noise_k(const ox_params *p, long step, double *noise_k) {
 /* ======================================================================= */
 
 static double *cplx_from_real(const double *r, long n, double *out) {
+#pragma omp parallel for schedule(static)
     for (long i = 0; i < n; i++) { out[2 * i] = r[i]; out[2 * i + 1] = 0.0; }
     return out;
 }
@@ -524,6 +525,62 @@ static double fe_of(const ox_params *p, const double *c2, const double *psi, con
     ox_power(p, psi, p3, 3, n);
     ox_power(p, psi, p4, 4, n);
     return ox_FE_calc(p, psi, p2, p3, p4, tmpc);
+}
+
+/* The stepping loop alone (no diagnostics), timed by wall clock; used as the
+   CPU baseline.  Returns the loop's seconds in *seconds. */
+int ox_bench(const ox_params *p, double *psi, long nsteps, double *seconds) {
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    const long n = (long)nx * ny * nz;
+    double *k2 = malloc(sizeof(double) * n), *c2 = malloc(sizeof(double) * n);
+    double *psi_k = malloc(sizeof(double) * 2 * n), *psi2_k = malloc(sizeof(double) * 2 * n);
+    double *psi3_k = malloc(sizeof(double) * 2 * n), *psi_kp1 = malloc(sizeof(double) * 2 * n);
+    double *p2 = malloc(sizeof(double) * n), *p3 = malloc(sizeof(double) * n);
+    double *noise = p->noise_amp != 0.0 ? malloc(sizeof(double) * 2 * n) : NULL;
+    if (!k2 || !c2 || !psi_k || !psi2_k || !psi3_k || !psi_kp1 || !p2 || !p3) return -1;
+    ox_k2_c2(p, k2, c2);
+    ox_fft3(cplx_from_real(psi, n, psi_k), nx, ny, nz, -1);
+    ox_power(p, psi, p2, 2, n);
+    ox_power(p, psi, p3, 3, n);
+#ifdef _OPENMP
+    double t0 = omp_get_wtime();
+#endif
+    for (long it = 0; it < nsteps; it++) {
+        ox_fft3(cplx_from_real(p2, n, psi2_k), nx, ny, nz, -1);
+        ox_fft3(cplx_from_real(p3, n, psi3_k), nx, ny, nz, -1);
+        ox_euler_step(p, k2, c2, psi_k, psi2_k, psi3_k, psi_kp1);
+        if (noise) {
+            ox_noise_k(p, it, noise);
+#pragma omp parallel for schedule(static)
+            for (long i = 0; i < n; i++) {
+                double den = (1.0 + k2[i] * p->dt * p->Mo * (1.0 - p->eps) - k2[i] * p->Mo * p->dt * c2[i]);
+                psi_kp1[2 * i] += noise[2 * i] / den;
+                psi_kp1[2 * i + 1] += noise[2 * i + 1] / den;
+            }
+        }
+        ox_fft3(psi_kp1, nx, ny, nz, +1);
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < n; i++) psi[i] = psi_kp1[2 * i] / (double)n;
+        ox_power(p, psi, p2, 2, n);
+        ox_power(p, psi, p3, 3, n);
+        ox_fft3(cplx_from_real(psi, n, psi_k), nx, ny, nz, -1);
+    }
+#ifdef _OPENMP
+    *seconds = omp_get_wtime() - t0;
+#else
+    *seconds = 0.0;
+#endif
+    free(k2); free(c2); free(psi_k); free(psi2_k); free(psi3_k); free(psi_kp1); free(p2); free(p3); free(noise);
+    return 0;
+}
+
+/* Threads the oracle's OpenMP regions use. */
+int ox_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
 }
 
 int ox_run(const ox_params *p, double *psi, long nsteps, int t_sample, ox_diag *diag) {

@@ -81,6 +81,9 @@ void ox_noise_k(const ox_params *p, long step, double *noise_k);
 /* Whole run mirroring main.cu:232-450.  psi: initial real field (mean already
    pinned), overwritten with the final field.  diag: nsteps+1 entries.       */
 int ox_run(const ox_params *p, double *psi, long nsteps, int t_sample, ox_diag *diag);
+/* The same loop without diagnostics, wall-clock timed (CPU baseline). */
+int ox_bench(const ox_params *p, double *psi, long nsteps, double *seconds);
+int ox_threads(void);
 
 /* Initial conditions ------------------------------------------------------ */
 /* Philox4x32-10 (Salmon et al., SC'11) and Box-Muller Gaussians. */

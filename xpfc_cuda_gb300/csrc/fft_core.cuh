@@ -1,0 +1,309 @@
+// fft_core.cuh -- complex arithmetic, register DFTs and the shared-memory
+// Stockham line FFT used by every pass of the XPFC step (sm_103a).
+//
+// A "line" is one 1-D transform of compile-time length L held in shared
+// memory with element stride ES (ES = 1 for rows, the tile width for column
+// tiles).  TPL threads cooperate on a line; every thread of the block runs the
+// same pass sequence, so passes are separated by __syncthreads().
+//
+// The Stockham autosort formulation (natural order in, natural order out):
+//   for each radix R (NS = product of earlier radices):
+//     butterfly j in [0, L/R): v[r] = x[j + r L/R] * W_{NS R}^{(j mod NS) r}
+//     DFT_R(v);  y[(j/NS) NS R + (j mod NS) + r NS] = v[r]
+// Twiddles come from a table W_L^k (k < L) computed in FP64 on the host and
+// rounded to the working type.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace xpfc {
+
+template <typename T> struct ctype;
+template <> struct ctype<float> { using type = float2; };
+template <> struct ctype<double> { using type = double2; };
+template <typename T> using cplx = typename ctype<T>::type;
+
+template <typename T> __device__ __forceinline__ cplx<T> mk(T x, T y) { cplx<T> r; r.x = x; r.y = y; return r; }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
+    return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// multiply by +i (s = +1) or -i (s = -1)
+template <int S> __device__ __forceinline__ float2 cmuli(float2 a) {
+    return S > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+template <int S> __device__ __forceinline__ double2 cmuli(double2 a) {
+    return S > 0 ? make_double2(-a.y, a.x) : make_double2(a.y, -a.x);
+}
+// twiddle multiply: forward (DIR=-1) uses w, inverse its conjugate
+template <int DIR, typename C> __device__ __forceinline__ C twmul(C a, C w) {
+    return DIR < 0 ? cmul(a, w) : cmulc(a, w);
+}
+
+// cos(pi k/8), sin(pi k/8) for k = 0..8, from the exact angles
+__host__ __device__ constexpr double c16c(int k) {
+    return k == 0 ? 1.0 : k == 1 ? 0.92387953251128675613 : k == 2 ? 0.70710678118654752440
+         : k == 3 ? 0.38268343236508977173 : k == 4 ? 0.0 : k == 5 ? -0.38268343236508977173
+         : k == 6 ? -0.70710678118654752440 : k == 7 ? -0.92387953251128675613 : -1.0;
+}
+__host__ __device__ constexpr double c16s(int k) { return c16c(k <= 4 ? 4 - k : k - 4) * (k <= 4 ? 1.0 : 1.0); }
+
+// ---------------------------------------------------------------------------
+// Register DFTs.  DIR = -1: X_k = sum x_n e^{-2 pi i nk/R}; DIR = +1: e^{+...}.
+// ---------------------------------------------------------------------------
+template <int DIR, typename C> __device__ __forceinline__ void dft2(C &a, C &b) {
+    C t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft4(C &x0, C &x1, C &x2, C &x3) {
+    C a = cadd(x0, x2), b = csub(x0, x2), c = cadd(x1, x3), d = csub(x1, x3);
+    // forward: X1 = b - i d, X3 = b + i d
+    C id = cmuli<DIR>(d);
+    x0 = cadd(a, c);
+    x2 = csub(a, c);
+    x1 = cadd(b, id);
+    x3 = csub(b, id);
+}
+
+template <int DIR, typename C, typename T> __device__ __forceinline__ C rot16(C a, int k) {
+    // a * W16^k for the forward direction (W16 = e^{-2 pi i/16}), conjugate for inverse
+    const T c = (T)c16c(k), s = (T)c16s(k);
+    return DIR < 0 ? mk<T>(a.x * c + a.y * s, a.y * c - a.x * s) : mk<T>(a.x * c - a.y * s, a.y * c + a.x * s);
+}
+
+template <int DIR, typename T> __device__ __forceinline__ void dft8(cplx<T> *v) {
+    // 8 = 2 x 4 (decimation in time): E = DFT4(even), O = DFT4(odd), X_k = E_k + W8^k O_k
+    dft4<DIR>(v[0], v[2], v[4], v[6]);
+    dft4<DIR>(v[1], v[3], v[5], v[7]);
+    cplx<T> o1 = rot16<DIR, cplx<T>, T>(v[3], 2);
+    cplx<T> o2 = cmuli<DIR>(v[5]);
+    cplx<T> o3 = rot16<DIR, cplx<T>, T>(v[7], 6);
+    cplx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    v[0] = cadd(e0, v[1]);
+    v[4] = csub(e0, v[1]);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+}
+
+// a * W16^e for e in [0, 9] (W16^9 = -W16^1)
+template <int DIR, typename T> __device__ __forceinline__ cplx<T> tw16(cplx<T> a, int e) {
+    if (e <= 8) return rot16<DIR, cplx<T>, T>(a, e);
+    cplx<T> r = rot16<DIR, cplx<T>, T>(a, e - 8);
+    return mk<T>(-r.x, -r.y);
+}
+
+template <int DIR, typename T> __device__ __forceinline__ void dft16(cplx<T> *v) {
+    // 16 = 4 x 4 with n = n1 + 4 n2, k = k2 + 4 k1:
+    // Y[n1][k2] = DFT4_n2(x[n1 + 4 n2]) * W16^{n1 k2};  X[k2 + 4 k1] = DFT4_n1(Y[n1][k2])
+    cplx<T> y[16];
+#pragma unroll
+    for (int n1 = 0; n1 < 4; n1++) {
+        cplx<T> a = v[n1], b = v[n1 + 4], c = v[n1 + 8], d = v[n1 + 12];
+        dft4<DIR>(a, b, c, d);
+        y[n1 * 4 + 0] = a;
+        y[n1 * 4 + 1] = tw16<DIR, T>(b, n1);
+        y[n1 * 4 + 2] = tw16<DIR, T>(c, 2 * n1);
+        y[n1 * 4 + 3] = tw16<DIR, T>(d, 3 * n1);
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) {
+        cplx<T> a = y[0 * 4 + k2], b = y[1 * 4 + k2], c = y[2 * 4 + k2], d = y[3 * 4 + k2];
+        dft4<DIR>(a, b, c, d);
+        v[k2] = a;
+        v[k2 + 4] = b;
+        v[k2 + 8] = c;
+        v[k2 + 12] = d;
+    }
+}
+
+template <int DIR, typename T> __device__ __forceinline__ void dft3(cplx<T> *v) {
+    const T h = (T)0.86602540378443864676;  // sqrt(3)/2
+    cplx<T> s = cadd(v[1], v[2]);
+    cplx<T> d = csub(v[1], v[2]);
+    cplx<T> m = mk<T>(v[0].x - (T)0.5 * s.x, v[0].y - (T)0.5 * s.y);
+    // forward: X1 = m - i h d, X2 = m + i h d
+    cplx<T> ihd = cmuli<DIR>(cscale(d, h));
+    v[0] = cadd(v[0], s);
+    v[1] = cadd(m, ihd);
+    v[2] = csub(m, ihd);
+}
+
+template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<T> *v) {
+    if constexpr (R == 2) dft2<DIR>(v[0], v[1]);
+    else if constexpr (R == 3) dft3<DIR, T>(v);
+    else if constexpr (R == 4) dft4<DIR>(v[0], v[1], v[2], v[3]);
+    else if constexpr (R == 8) dft8<DIR, T>(v);
+    else if constexpr (R == 16) dft16<DIR, T>(v);
+    else static_assert(R == 2, "unsupported radix");
+}
+
+// ---------------------------------------------------------------------------
+// Radix plan: 3s first, then 16s, finishing the power of two with 8/4/2
+// (2^(4q+1) uses 8*4 for its last 16*2).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int radix_at(int L, int p) {
+    // radix of pass p for length L
+    int rem = L;
+    for (int q = 0;; q++) {
+        int r = 1;
+        if (rem % 3 == 0) r = 3;
+        else if (rem == 32) r = 8;
+        else if (rem % 16 == 0) r = 16;
+        else if (rem % 8 == 0) r = 8;
+        else if (rem % 4 == 0) r = 4;
+        else if (rem % 2 == 0) r = 2;
+        else r = 1;
+        if (q == p) return r;
+        if (r == 1) return 1;
+        rem /= r;
+    }
+}
+__host__ __device__ constexpr int num_passes(int L) {
+    int n = 0;
+    while (radix_at(L, n) != 1) n++;
+    return n;
+}
+__host__ __device__ constexpr int ns_at(int L, int p) {
+    int ns = 1;
+    for (int q = 0; q < p; q++) ns *= radix_at(L, q);
+    return ns;
+}
+__host__ __device__ constexpr int cdiv(int a, int b) { return (a + b - 1) / b; }
+// registers (complex values) a thread needs for any pass of length L with TPL threads
+__host__ __device__ constexpr int max_regs(int L, int TPL) {
+    int m = 0;
+    for (int p = 0; p < num_passes(L); p++) {
+        int R = radix_at(L, p);
+        int v = cdiv(L / R, TPL) * R;
+        m = v > m ? v : m;
+    }
+    return m;
+}
+
+// Shared-memory index of element e of a line: rows use a skew of one slot
+// per 128 bytes so that stride-R Stockham writes hit distinct banks.
+template <typename T, int ES> struct LineIdx {
+    static constexpr int SK = (sizeof(cplx<T>) == 8) ? 4 : 3;
+    __device__ __forceinline__ static int at(int e) {
+        if constexpr (ES == 1) return e + (e >> SK);
+        else return e * ES;
+    }
+    __host__ __device__ static constexpr int span(int L) { return ES == 1 ? L + (L >> SK) + 1 : L * ES; }
+};
+
+// One Stockham pass of radix R on every line of the block.
+template <typename T, int L, int P, int DIR, int TPL, int ES>
+__device__ __forceinline__ void stockham_pass(cplx<T> *line, int t, const cplx<T> *__restrict__ tw) {
+    constexpr int R = radix_at(L, P);
+    constexpr int NS = ns_at(L, P);
+    constexpr int NB = L / R;
+    constexpr int PER = cdiv(NB, TPL);
+    constexpr int TWS = L / (NS * R);
+    using I = LineIdx<T, ES>;
+    cplx<T> v[PER][R];
+#pragma unroll
+    for (int b = 0; b < PER; b++) {
+        const int j = t + b * TPL;
+        if (PER * TPL == NB || j < NB) {
+            const int k = j % NS;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                cplx<T> x = line[I::at(j + r * NB)];
+                if (NS > 1 && r > 0) x = twmul<DIR>(x, tw[k * r * TWS]);
+                v[b][r] = x;
+            }
+            dftR<R, DIR, T>(v[b]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < PER; b++) {
+        const int j = t + b * TPL;
+        if (PER * TPL == NB || j < NB) {
+            const int k = j % NS;
+            const int d = (j / NS) * NS * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++) line[I::at(d + r * NS)] = v[b][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int L, int P, int DIR, int TPL, int ES>
+__device__ __forceinline__ void line_fft_from(cplx<T> *line, int t, const cplx<T> *__restrict__ tw) {
+    if constexpr (P < num_passes(L)) {
+        stockham_pass<T, L, P, DIR, TPL, ES>(line, t, tw);
+        line_fft_from<T, L, P + 1, DIR, TPL, ES>(line, t, tw);
+    }
+}
+
+// Full unnormalised L-point FFT of the line (natural order in and out).
+// The caller must __syncthreads() before (data ready); returns synchronised.
+template <typename T, int L, int DIR, int TPL, int ES>
+__device__ __forceinline__ void line_fft(cplx<T> *line, int t, const cplx<T> *__restrict__ tw) {
+    line_fft_from<T, L, 0, DIR, TPL, ES>(line, t, tw);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 block reduction (warp shuffles, then one value per warp in shared
+// memory).  Deterministic for a fixed block size.
+// ---------------------------------------------------------------------------
+template <int NQ>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NQ], double *__restrict__ out, double *sred) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NQ; q++) sred[warp * NQ + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x < NQ) {
+        double s = 0.0;
+        for (int w = 0; w < nwarps; w++) s += sred[w * NQ + threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and Box-Muller.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+}  // namespace xpfc

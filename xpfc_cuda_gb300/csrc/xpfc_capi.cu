@@ -1,0 +1,1001 @@
+// xpfc_capi.cu -- the C ABI of libxpfc (include/xpfc.h): context, fused
+// step driver and the staged per-stage entry points.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/xpfc.h"
+#include "xpfc_host.h"
+#include "xpfc_launch.h"
+
+using namespace xpfc;
+
+struct xpfc_ctx {
+    xpfc_params p;
+    int n0, n1, n2, L0, three_d;
+    double Lax[3];
+    long long ncells;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    // fused state (T = float for XPFC_MIXED, double for XPFC_FP64)
+    void *S = nullptr, *W = nullptr, *X = nullptr;
+    size_t esz = 8;
+    // twiddle tables W_L^k (k < L), keyed by (L, is_double)
+    std::map<long long, void *> tw;
+    // per-shell coefficient tables
+    void *table_f = nullptr, *table_d = nullptr;
+    int mmax = 0;
+    double *partials = nullptr;
+    size_t partials_cap = 0;
+    double *slots = nullptr;
+    double *hslots = nullptr;
+    int slots_cap = 0;
+    double *init_red = nullptr;
+    double *staged[XPFC_NBUF] = {nullptr};
+    long long iteration = 0;
+    bool initialized = false;
+    long long launches = 0;
+    void *hstage = nullptr;
+    size_t hstage_bytes = 0;
+    // diagnostics schedule of the last step call
+    std::vector<long long> diag_its;
+    long long diag_it0 = 0, diag_fin = 0;
+    bool diag_final = false, diag_pending = false;
+    // per-pass profiling with CUDA events
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> ev_used;   // (pass, pool index of the start event)
+    double prof_ms[8] = {0};
+    long long prof_n[8] = {0};
+};
+
+enum { PASS_PENCIL = 0, PASS_COL_INV = 1, PASS_ROW = 2, PASS_COL_FWD = 3, PASS_RED = 4 };
+
+// brackets one launch with a pair of pooled events when profiling is on
+struct ProfScope {
+    xpfc_ctx *c;
+    int pass, idx = -1;
+    ProfScope(xpfc_ctx *ctx, int ps) : c(ctx), pass(ps) {
+        if (!c->profiling) return;
+        const int used = (int)c->ev_used.size() * 2;
+        if (used + 2 > (int)c->ev_pool.size()) return;
+        idx = used;
+        cudaEventRecord(c->ev_pool[idx], c->stream);
+    }
+    ~ProfScope() {
+        if (idx < 0) return;
+        cudaEventRecord(c->ev_pool[idx + 1], c->stream);
+        c->ev_used.push_back({pass, idx});
+    }
+};
+
+static void drain_profile(xpfc_ctx *c) {
+    if (c->ev_used.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto &u : c->ev_used) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev_pool[u.second], c->ev_pool[u.second + 1]) == cudaSuccess) {
+            c->prof_ms[u.first] += ms;
+            c->prof_n[u.first]++;
+        }
+    }
+    c->ev_used.clear();
+}
+
+static const char *kVersion = "xpfc-gb300 0.1 (sm_103a)";
+
+#define XPFC_CUDA(ctx, call)                                                                      \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                      \
+            return XPFC_ECUDA;                                                                    \
+        }                                                                                         \
+    } while (0)
+
+#define XPFC_LAUNCH(ctx, call)   \
+    do {                         \
+        (ctx)->launches++;       \
+        XPFC_CUDA(ctx, call);    \
+    } while (0)
+
+static int fail(xpfc_ctx *ctx, int code, const std::string &m) {
+    if (ctx) ctx->err = m;
+    else set_thread_error(m);
+    return code;
+}
+
+// ---------------------------------------------------------------------------
+// parameters
+// ---------------------------------------------------------------------------
+extern "C" int xpfc_default_params(xpfc_params *p) {
+    if (!p) return XPFC_EINVAL;
+    memset(p, 0, sizeof(*p));
+    p->Mx = p->My = p->Mz = 64;
+    p->Lx = p->Ly = p->Lz = 8.0;
+    p->psi0 = 0.05;
+    p->sigma = 0.1;
+    p->a = 1.0;           // eta = 2
+    p->b = 1.0 / 3.0;     // chi = 1
+    p->eps = 0.0;
+    p->Mo = 1.0;
+    p->dt = 1.0;
+    p->nsteps = 2001;
+    p->t_sample = 100;
+    p->npeaks = 1;
+    p->pk_k[0] = 2.0 * M_PI;
+    p->pk_alpha[0] = 1.0;
+    p->pk_rho[0] = 1.0;
+    p->pk_beta[0] = 8.0;
+    p->envelope = XPFC_ENVELOPE_MAX;
+    p->precision = XPFC_FP64;
+    p->ref_compat = 0;
+    p->ff_factor = (8.0 / 64) * (8.0 / 64) * (8.0 / 64);
+    p->ic_kind = XPFC_IC_NOISE;
+    p->iconfig = 2;
+    p->ic_amp = 0.1;
+    p->ic_seed = 1;
+    p->noise_seed = 1;
+    p->device = 0;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_read_input(const char *path, xpfc_params *p) {
+    if (!path || !p) return fail(nullptr, XPFC_EINVAL, "null argument");
+    return read_input(path, p);
+}
+
+extern "C" const char *xpfc_version(void) { return kVersion; }
+
+extern "C" const char *xpfc_last_error(const xpfc_ctx *ctx) { return ctx ? ctx->err.c_str() : thread_error(); }
+
+extern "C" int xpfc_get_params(const xpfc_ctx *ctx, xpfc_params *p) {
+    if (!ctx || !p) return XPFC_EINVAL;
+    *p = ctx->p;
+    return XPFC_OK;
+}
+
+extern "C" void *xpfc_get_stream(const xpfc_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" long long xpfc_launch_count(const xpfc_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" long long xpfc_iteration(const xpfc_ctx *ctx) { return ctx ? ctx->iteration : -1; }
+
+extern "C" int xpfc_build_initial_field(const xpfc_params *p, double *host_psi) {
+    if (!p || !host_psi) return fail(nullptr, XPFC_EINVAL, "null argument");
+    return build_initial_field(p, host_psi);
+}
+
+extern "C" int xpfc_write_vtk(const char *path, const double *psi, int Mx, int My, int Mz, double Lx, double Ly,
+                              double Lz, int precision) {
+    if (!path || !psi || Mx <= 0 || My <= 0 || Mz <= 0) return fail(nullptr, XPFC_EINVAL, "bad argument");
+    return write_vtk(path, psi, Mx, My, Mz, Lx, Ly, Lz, precision);
+}
+
+extern "C" int xpfc_read_vtk(const char *path, double *psi, size_t cap, int dims[3], double L[3]) {
+    if (!path) return fail(nullptr, XPFC_EINVAL, "null path");
+    return read_vtk(path, psi, cap, dims, L);
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+static double c2_of(const xpfc_params &p, double kmag) {
+    // initialize.cu:209-217 (sum) and its max envelope
+    double acc = 0.0;
+    for (int i = 0; i < p.npeaks; i++) {
+        const double sk = p.sigma * p.pk_k[i];
+        const double dw = std::exp(-(sk * sk) / (2.0 * p.pk_rho[i] * p.pk_beta[i]));
+        const double d = kmag - p.pk_k[i];
+        const double v = dw * std::exp(-(d * d) / (2.0 * p.pk_alpha[i] * p.pk_alpha[i]));
+        if (p.envelope == XPFC_ENVELOPE_SUM) acc += v;
+        else acc = (i == 0 || v > acc) ? v : acc;
+    }
+    return acc;
+}
+
+static void *twiddle(xpfc_ctx *ctx, int L, bool dbl) {
+    const long long key = 2LL * L + (dbl ? 1 : 0);
+    auto it = ctx->tw.find(key);
+    if (it != ctx->tw.end()) return it->second;
+    std::vector<double> h(2 * (size_t)L);
+    for (int k = 0; k < L; k++) {
+        const double ang = 2.0 * M_PI * (double)k / (double)L;
+        h[2 * k] = std::cos(ang);
+        h[2 * k + 1] = -std::sin(ang);
+    }
+    void *d = nullptr;
+    if (dbl) {
+        if (cudaMalloc(&d, sizeof(double) * 2 * L) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, h.data(), sizeof(double) * 2 * L, cudaMemcpyHostToDevice);
+    } else {
+        std::vector<float> f(2 * (size_t)L);
+        for (size_t i = 0; i < f.size(); i++) f[i] = (float)h[i];
+        if (cudaMalloc(&d, sizeof(float) * 2 * L) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, f.data(), sizeof(float) * 2 * L, cudaMemcpyHostToDevice);
+    }
+    ctx->tw[key] = d;
+    return d;
+}
+
+static KSpace make_kspace(const xpfc_ctx *ctx, bool dbl) {
+    const xpfc_params &p = ctx->p;
+    KSpace ks;
+    memset(&ks, 0, sizeof(ks));
+    ks.n0 = ctx->n0;
+    ks.n1 = ctx->n1;
+    ks.n2 = ctx->n2;
+    const double d0 = 2.0 * M_PI / ctx->Lax[0], d1 = 2.0 * M_PI / ctx->Lax[1], d2 = 2.0 * M_PI / ctx->Lax[2];
+    ks.dk0sq = d0 * d0;
+    ks.dk1sq = d1 * d1;
+    ks.dk2sq = ctx->n2 > 1 ? d2 * d2 : 0.0;
+    ks.table = dbl ? ctx->table_d : ctx->table_f;
+    ks.mmax = ctx->mmax;
+    ks.dt = p.dt;
+    ks.Mo = p.Mo;
+    ks.Mo_res = p.ref_compat ? (double)(int)p.Mo : p.Mo;   // sse_calculation.cu:120 takes int Mo
+    ks.eps = p.eps;
+    ks.npeaks = p.npeaks;
+    ks.envelope = p.envelope;
+    for (int i = 0; i < p.npeaks && i < 8; i++) {
+        const double sk = p.sigma * p.pk_k[i];
+        ks.pk_k[i] = p.pk_k[i];
+        ks.pk_inv2a2[i] = 1.0 / (2.0 * p.pk_alpha[i] * p.pk_alpha[i]);
+        ks.pk_dw[i] = std::exp(-(sk * sk) / (2.0 * p.pk_rho[i] * p.pk_beta[i]));
+    }
+    ks.noise_on = p.noise_amp != 0.0;
+    ks.noise_scale = p.noise_amp * std::sqrt((double)ctx->ncells);
+    ks.noise_seed = p.noise_seed;
+    return ks;
+}
+
+static int build_tables(xpfc_ctx *ctx) {
+    // one coefficient set per shell m = i0^2 + i1^2 + i2^2 when the k-grid
+    // spacing is the same on every axis (equal box lengths)
+    const bool cubic = (ctx->Lax[0] == ctx->Lax[1]) && (ctx->n2 == 1 || ctx->Lax[0] == ctx->Lax[2]);
+    if (!cubic) return XPFC_OK;
+    const int h0 = ctx->n0 / 2, h1 = ctx->n1 / 2, h2 = ctx->n2 / 2;
+    ctx->mmax = h0 * h0 + h1 * h1 + h2 * h2;
+    const size_t nm = (size_t)ctx->mmax + 1;
+    std::vector<double> td(4 * nm);
+    std::vector<float> tf(4 * nm);
+    const double dk = 2.0 * M_PI / ctx->Lax[0];
+    const xpfc_params &p = ctx->p;
+    for (size_t m = 0; m < nm; m++) {
+        const double k2 = dk * dk * (double)m;
+        const double c2 = c2_of(p, std::sqrt(k2));
+        const double den = (1.0 + k2 * p.dt * p.Mo * (1.0 - p.eps) - k2 * p.Mo * p.dt * c2);
+        td[4 * m + 0] = 1.0 / den;
+        td[4 * m + 1] = -(k2 * p.Mo * p.dt) / den;
+        td[4 * m + 2] = c2;
+        td[4 * m + 3] = k2;
+        for (int j = 0; j < 4; j++) tf[4 * m + j] = (float)td[4 * m + j];
+    }
+    XPFC_CUDA(ctx, cudaMalloc(&ctx->table_d, sizeof(double) * td.size()));
+    XPFC_CUDA(ctx, cudaMalloc(&ctx->table_f, sizeof(float) * tf.size()));
+    XPFC_CUDA(ctx, cudaMemcpy(ctx->table_d, td.data(), sizeof(double) * td.size(), cudaMemcpyHostToDevice));
+    XPFC_CUDA(ctx, cudaMemcpy(ctx->table_f, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice));
+    return XPFC_OK;
+}
+
+static int ensure_partials(xpfc_ctx *ctx, size_t n) {
+    if (n <= ctx->partials_cap) return XPFC_OK;
+    if (ctx->partials) cudaFree(ctx->partials);
+    ctx->partials = nullptr;
+    XPFC_CUDA(ctx, cudaMalloc(&ctx->partials, sizeof(double) * n));
+    ctx->partials_cap = n;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_create(const xpfc_params *p, xpfc_ctx **out) {
+    if (!p || !out) return fail(nullptr, XPFC_EINVAL, "null argument");
+    *out = nullptr;
+    if (p->Mx <= 0 || p->My <= 0 || p->Mz <= 0) return fail(nullptr, XPFC_EINVAL, "grid sizes must be positive");
+    if (p->dt <= 0.0 || p->npeaks < 1 || p->npeaks > XPFC_MAX_PEAKS)
+        return fail(nullptr, XPFC_EINVAL, "dt must be > 0 and 1 <= npeaks <= 8");
+    if (p->precision != XPFC_FP64 && p->precision != XPFC_MIXED) return fail(nullptr, XPFC_EINVAL, "bad precision");
+    xpfc_ctx *ctx = new xpfc_ctx();
+    ctx->p = *p;
+    ctx->three_d = p->Mz > 1;
+    if (ctx->three_d) {
+        ctx->n0 = p->Mz; ctx->n1 = p->My; ctx->n2 = p->Mx;
+        ctx->Lax[0] = p->Lz; ctx->Lax[1] = p->Ly; ctx->Lax[2] = p->Lx;
+    } else {
+        ctx->n0 = p->My; ctx->n1 = p->Mx; ctx->n2 = 1;
+        ctx->Lax[0] = p->Ly; ctx->Lax[1] = p->Lx; ctx->Lax[2] = 1.0;
+    }
+    ctx->L0 = ctx->n0 / 2;
+    ctx->ncells = (long long)ctx->n0 * ctx->n1 * ctx->n2;
+    auto reject = [&](const std::string &m) {
+        set_thread_error(m);
+        delete ctx;
+        return XPFC_EINVAL;
+    };
+    if (ctx->n0 % 2 != 0 || ctx->n1 % 2 != 0 || (ctx->three_d && ctx->n2 % 2 != 0))
+        return reject("grid sizes must be even");
+    if (!row_supported(ctx->L0)) return reject("unsupported size of the fastest axis: " + std::to_string(ctx->n0));
+    if (!col_supported(ctx->n1)) return reject("unsupported axis length " + std::to_string(ctx->n1));
+    if (ctx->three_d && (!col_supported(ctx->n2) || !pen_supported(ctx->n2, 2)))
+        return reject("unsupported axis length " + std::to_string(ctx->n2));
+    if (!ctx->three_d && !pen_supported(ctx->n1, 1)) return reject("unsupported axis length " + std::to_string(ctx->n1));
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e != cudaSuccess) {
+        set_thread_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        delete ctx;
+        return XPFC_ECUDA;
+    }
+    if (p->stream) {
+        ctx->stream = (cudaStream_t)p->stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            set_thread_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+            delete ctx;
+            return XPFC_ECUDA;
+        }
+        ctx->own_stream = true;
+    }
+    ctx->esz = p->precision == XPFC_MIXED ? sizeof(float) : sizeof(double);
+    const size_t bytes = ctx->esz * (size_t)ctx->ncells;
+    int rc = XPFC_OK;
+    if (cudaMalloc(&ctx->S, bytes) != cudaSuccess || cudaMalloc(&ctx->W, bytes) != cudaSuccess) {
+        set_thread_error("device allocation of the state failed");
+        xpfc_destroy(ctx);
+        return XPFC_ENOMEM;
+    }
+    rc = build_tables(ctx);
+    if (rc == XPFC_OK) {
+        const int L0 = ctx->L0;
+        const size_t rowblk = (size_t)ctx->n1 * ctx->n2 / row_rows(L0) + 1;
+        const int tx = ctx->esz == 4 ? (ctx->three_d ? pen_tx<float>(ctx->n2, 2) : pen_tx<float>(ctx->n1, 1))
+                                     : (ctx->three_d ? pen_tx<double>(ctx->n2, 2) : pen_tx<double>(ctx->n1, 1));
+        const size_t penblk = (size_t)(L0 / tx + 1) * (ctx->n1 / 2 + 1);
+        size_t need = std::max(rowblk * NQ_ROW, penblk * NQ_PEN);
+        need = std::max(need, (size_t)DENSITY_BLOCKS);
+        rc = ensure_partials(ctx, need);
+    }
+    if (rc == XPFC_OK && cudaMalloc(&ctx->init_red, sizeof(double) * 8) != cudaSuccess) rc = XPFC_ENOMEM;
+    if (rc != XPFC_OK) {
+        set_thread_error(ctx->err.empty() ? "context set-up failed" : ctx->err);
+        xpfc_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_destroy(xpfc_ctx *ctx) {
+    if (!ctx) return XPFC_OK;
+    cudaSetDevice(ctx->p.device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->S);
+    cudaFree(ctx->W);
+    cudaFree(ctx->X);
+    for (auto &kv : ctx->tw) cudaFree(kv.second);
+    cudaFree(ctx->table_f);
+    cudaFree(ctx->table_d);
+    cudaFree(ctx->partials);
+    cudaFree(ctx->slots);
+    cudaFree(ctx->init_red);
+    if (ctx->hslots) cudaFreeHost(ctx->hslots);
+    if (ctx->hstage) cudaFreeHost(ctx->hstage);
+    for (int b = 0; b < XPFC_NBUF; b++) cudaFree(ctx->staged[b]);
+    for (auto &e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return XPFC_OK;
+}
+
+static int host_stage(xpfc_ctx *ctx, size_t bytes) {
+    if (bytes <= ctx->hstage_bytes) return XPFC_OK;
+    if (ctx->hstage) cudaFreeHost(ctx->hstage);
+    ctx->hstage = nullptr;
+    XPFC_CUDA(ctx, cudaMallocHost(&ctx->hstage, bytes));
+    ctx->hstage_bytes = bytes;
+    return XPFC_OK;
+}
+
+static double *staged_buf(xpfc_ctx *ctx, int b) {
+    if (b < 0 || b >= XPFC_NBUF) return nullptr;
+    if (!ctx->staged[b]) {
+        if (cudaMalloc(&ctx->staged[b], sizeof(double) * (size_t)ctx->ncells) != cudaSuccess) return nullptr;
+        cudaMemsetAsync(ctx->staged[b], 0, sizeof(double) * (size_t)ctx->ncells, ctx->stream);
+    }
+    return ctx->staged[b];
+}
+
+// ---------------------------------------------------------------------------
+// transforms on one field buffer of type T (packed spectrum <-> real)
+// ---------------------------------------------------------------------------
+template <typename T>
+static int fft_forward_xy(xpfc_ctx *ctx, void *buf, bool do_rows) {
+    const bool dbl = sizeof(T) == 8;
+    void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl), *tw1 = twiddle(ctx, ctx->n1, dbl);
+    if (!tw0 || !tw2 || !tw1) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+    if (do_rows) {
+        RowArgs ra{};
+        ra.in = buf;
+        ra.out = buf;
+        ra.nrows = (long long)ctx->n1 * ctx->n2;
+        ra.scale = 1.0;
+        XPFC_LAUNCH(ctx, launch_row<T>(ROW_FWD, ctx->L0, ra, tw0, tw2, ctx->stream, nullptr));
+    }
+    ColArgs ca{};
+    ca.in = buf;
+    ca.out = buf;
+    ca.es = ctx->L0;
+    ca.ostride = (long long)ctx->n1 * ctx->L0;
+    ca.scale = 1.0;
+    ca.ncols = ctx->L0;
+    XPFC_LAUNCH(ctx, launch_col<T>(-1, ctx->n1, ca, ctx->n2, tw1, ctx->stream));
+    return XPFC_OK;
+}
+
+template <typename T>
+static int fft_full(xpfc_ctx *ctx, void *buf, int dir) {
+    const bool dbl = sizeof(T) == 8;
+    void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl), *tw1 = twiddle(ctx, ctx->n1, dbl);
+    void *twz = ctx->three_d ? twiddle(ctx, ctx->n2, dbl) : nullptr;
+    if (!tw0 || !tw2 || !tw1 || (ctx->three_d && !twz)) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+    RowArgs ra{};
+    ra.in = buf;
+    ra.out = buf;
+    ra.nrows = (long long)ctx->n1 * ctx->n2;
+    ra.scale = 1.0;
+    ColArgs cy{};
+    cy.in = buf;
+    cy.out = buf;
+    cy.es = ctx->L0;
+    cy.ostride = (long long)ctx->n1 * ctx->L0;
+    cy.scale = 1.0;
+    cy.ncols = ctx->L0;
+    ColArgs cz{};
+    cz.in = buf;
+    cz.out = buf;
+    cz.es = (long long)ctx->n1 * ctx->L0;
+    cz.ostride = ctx->L0;
+    cz.scale = 1.0;
+    cz.ncols = ctx->L0;
+    if (dir < 0) {
+        XPFC_LAUNCH(ctx, launch_row<T>(ROW_FWD, ctx->L0, ra, tw0, tw2, ctx->stream, nullptr));
+        XPFC_LAUNCH(ctx, launch_col<T>(-1, ctx->n1, cy, ctx->n2, tw1, ctx->stream));
+        if (ctx->three_d) XPFC_LAUNCH(ctx, launch_col<T>(-1, ctx->n2, cz, ctx->n1, twz, ctx->stream));
+    } else {
+        if (ctx->three_d) XPFC_LAUNCH(ctx, launch_col<T>(1, ctx->n2, cz, ctx->n1, twz, ctx->stream));
+        XPFC_LAUNCH(ctx, launch_col<T>(1, ctx->n1, cy, ctx->n2, tw1, ctx->stream));
+        XPFC_LAUNCH(ctx, launch_row<T>(ROW_INV, ctx->L0, ra, tw0, tw2, ctx->stream, nullptr));
+    }
+    return XPFC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// initialisation of both the staged buffers and the fused state
+// ---------------------------------------------------------------------------
+template <typename T>
+static int init_fused(xpfc_ctx *ctx, const double *dpsi) {
+    const bool dbl = sizeof(T) == 8;
+    const long long n = ctx->ncells;
+    if (dbl) XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->S, dpsi, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    else XPFC_LAUNCH(ctx, launch_convert_d2f(dpsi, (float *)ctx->S, n, ctx->stream));
+    void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl);
+    if (!tw0 || !tw2) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+    // W = row transform of N(psi), with the iteration-0 real-space sums
+    RowArgs ra{};
+    ra.in = ctx->S;
+    ra.out = ctx->W;
+    ra.nrows = (long long)ctx->n1 * ctx->n2;
+    ra.a = ctx->p.a;
+    ra.b = ctx->p.b;
+    ra.scale = 1.0;
+    ra.partials = ctx->partials;
+    ra.want_red = 1;
+    ra.ref_compat = ctx->p.ref_compat;
+    int nb = 0;
+    XPFC_LAUNCH(ctx, launch_row<T>(ROW_NL_FWD, ctx->L0, ra, tw0, tw2, ctx->stream, &nb));
+    XPFC_LAUNCH(ctx, launch_finalize(NQ_ROW, ctx->partials, nb, ctx->init_red, ctx->stream));
+    int rc = fft_forward_xy<T>(ctx, ctx->S, true);
+    if (rc != XPFC_OK) return rc;
+    if (ctx->three_d) {
+        rc = fft_forward_xy<T>(ctx, ctx->W, false);
+        if (rc != XPFC_OK) return rc;
+    }
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    const size_t n = (size_t)ctx->ncells;
+    int rc = host_stage(ctx, sizeof(double) * n);
+    if (rc != XPFC_OK) return rc;
+    double *h = (double *)ctx->hstage;
+    if (host_psi) {
+        memcpy(h, host_psi, sizeof(double) * n);
+        pin_mean(h, n, ctx->p.psi0);          // configure_avg_density, Avg_calc.cu:21-43
+    } else {
+        rc = build_initial_field(&ctx->p, h);
+        if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
+    }
+    double *dpsi = staged_buf(ctx, XPFC_BUF_PSI);
+    if (!dpsi) return fail(ctx, XPFC_ENOMEM, "staged buffer allocation failed");
+    XPFC_CUDA(ctx, cudaMemcpyAsync(dpsi, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
+    if (rc != XPFC_OK) return rc;
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->iteration = 0;
+    ctx->initialized = true;
+    return XPFC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fused step
+// ---------------------------------------------------------------------------
+template <typename T>
+static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int want_red, int *nb) {
+    const bool dbl = sizeof(T) == 8;
+    const int Lp = ctx->three_d ? ctx->n2 : ctx->n1;
+    void *twp = twiddle(ctx, Lp, dbl);
+    if (!twp) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+    KSpace ks = make_kspace(ctx, dbl);
+    ks.step = step;
+    PenArgs pa{};
+    pa.S = ctx->S;
+    pa.W = ctx->W;
+    pa.es = ctx->three_d ? (long long)ctx->n1 * ctx->L0 : ctx->L0;
+    pa.gstride = ctx->three_d ? ctx->L0 : 0;
+    pa.three_d = ctx->three_d;
+    pa.L0 = ctx->L0;
+    pa.scale = 1.0 / Lp;
+    pa.update = update;
+    pa.want_red = want_red;
+    pa.partials = ctx->partials;
+    pa.pin = (!dbl) ? 1 : 0;
+    pa.pin_value = ctx->p.psi0 * (double)ctx->ncells;
+    const int npairs = ctx->three_d ? ctx->n1 / 2 + 1 : 1;
+    ProfScope ps(ctx, PASS_PENCIL);
+    XPFC_LAUNCH(ctx, launch_pencil<T>(Lp, ctx->three_d ? 2 : 1, pa, ks, npairs, twp, ctx->stream, nb));
+    return XPFC_OK;
+}
+
+template <typename T>
+static int launch_xy_pass(xpfc_ctx *ctx, int want_red, int *nb) {
+    const bool dbl = sizeof(T) == 8;
+    void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl);
+    if (!tw0 || !tw2) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+    RowArgs ra{};
+    ra.nrows = (long long)ctx->n1 * ctx->n2;
+    ra.a = ctx->p.a;
+    ra.b = ctx->p.b;
+    ra.partials = ctx->partials;
+    ra.want_red = want_red;
+    ra.ref_compat = ctx->p.ref_compat;
+    if (ctx->three_d) {
+        void *tw1 = twiddle(ctx, ctx->n1, dbl);
+        if (!tw1) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+        ColArgs cy{};
+        cy.in = ctx->S;
+        cy.out = ctx->W;
+        cy.es = ctx->L0;
+        cy.ostride = (long long)ctx->n1 * ctx->L0;
+        cy.scale = 1.0;
+        cy.ncols = ctx->L0;
+        {
+            ProfScope ps(ctx, PASS_COL_INV);
+            XPFC_LAUNCH(ctx, launch_col<T>(1, ctx->n1, cy, ctx->n2, tw1, ctx->stream));
+        }
+        ra.in = ctx->W;
+        ra.out = ctx->W;
+        ra.scale = 1.0 / ((double)ctx->n0 * ctx->n1);
+        {
+            ProfScope ps(ctx, PASS_ROW);
+            XPFC_LAUNCH(ctx, launch_row<T>(ROW_FUSED, ctx->L0, ra, tw0, tw2, ctx->stream, nb));
+        }
+        cy.in = ctx->W;
+        {
+            ProfScope ps(ctx, PASS_COL_FWD);
+            XPFC_LAUNCH(ctx, launch_col<T>(-1, ctx->n1, cy, ctx->n2, tw1, ctx->stream));
+        }
+    } else {
+        ra.in = ctx->S;
+        ra.out = ctx->W;
+        ra.scale = 1.0 / (double)ctx->n0;
+        ProfScope ps(ctx, PASS_ROW);
+        XPFC_LAUNCH(ctx, launch_row<T>(ROW_FUSED, ctx->L0, ra, tw0, tw2, ctx->stream, nb));
+    }
+    return XPFC_OK;
+}
+
+static bool diag_wantF(const xpfc_ctx *ctx, long long i) {
+    const int ts = ctx->p.t_sample;
+    if (i == ctx->diag_it0) return ctx->diag_it0 == 0;
+    return (ctx->diag_final && i == ctx->diag_fin) || (ts > 0 && i % ts == 0);
+}
+static bool diag_wantR(const xpfc_ctx *ctx, long long i) {
+    const int ts = ctx->p.t_sample;
+    return i < ctx->diag_fin && ts > 0 && i % ts == 0;
+}
+
+// Enqueues nsteps iterations with their diagnostics into device slots.
+template <typename T>
+static int fused_enqueue(xpfc_ctx *ctx, long long nsteps, bool final_F) {
+    const long long it0 = ctx->iteration, fin = it0 + nsteps;
+    const int ts = ctx->p.t_sample;
+    ctx->diag_it0 = it0;
+    ctx->diag_fin = fin;
+    ctx->diag_final = final_F;
+    std::vector<long long> &its = ctx->diag_its;
+    its.clear();
+    std::map<long long, int> slot;
+    auto add = [&](long long i) {
+        if (!slot.count(i)) {
+            slot[i] = (int)its.size();
+            its.push_back(i);
+        }
+    };
+    if (diag_wantF(ctx, it0) || diag_wantR(ctx, it0)) add(it0);
+    if (ts > 0)
+        for (long long i = ((it0 / ts) + 1) * ts; i <= fin; i += ts)
+            if (diag_wantF(ctx, i) || diag_wantR(ctx, i)) add(i);
+    if (final_F) add(fin);
+    const int ns = (int)its.size();
+    if (ns > ctx->slots_cap) {
+        cudaFree(ctx->slots);
+        if (ctx->hslots) cudaFreeHost(ctx->hslots);
+        ctx->slots = nullptr;
+        ctx->hslots = nullptr;
+        XPFC_CUDA(ctx, cudaMalloc(&ctx->slots, sizeof(double) * 8 * ns));
+        XPFC_CUDA(ctx, cudaMallocHost(&ctx->hslots, sizeof(double) * 8 * ns));
+        ctx->slots_cap = ns;
+    }
+    if (ns > 0) XPFC_CUDA(ctx, cudaMemsetAsync(ctx->slots, 0, sizeof(double) * 8 * ns, ctx->stream));
+    if (it0 == 0 && slot.count(0))
+        XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->slots + 8 * slot[0], ctx->init_red, sizeof(double) * NQ_ROW,
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+    for (long long i = it0; i < fin; i++) {
+        const bool red = diag_wantF(ctx, i) || diag_wantR(ctx, i);
+        int nb = 0;
+        int rc = launch_pencil_pass<T>(ctx, i, 1, red ? 1 : 0, &nb);
+        if (rc != XPFC_OK) return rc;
+        if (red) {
+            ProfScope ps(ctx, PASS_RED);
+            XPFC_LAUNCH(ctx, launch_finalize(NQ_PEN, ctx->partials, nb, ctx->slots + 8 * slot[i] + 4, ctx->stream));
+        }
+        const bool redl = diag_wantF(ctx, i + 1);
+        rc = launch_xy_pass<T>(ctx, redl ? 1 : 0, &nb);
+        if (rc != XPFC_OK) return rc;
+        if (redl) {
+            ProfScope ps(ctx, PASS_RED);
+            XPFC_LAUNCH(ctx, launch_finalize(NQ_ROW, ctx->partials, nb, ctx->slots + 8 * slot[i + 1], ctx->stream));
+        }
+    }
+    if (final_F && diag_wantF(ctx, fin)) {
+        // the final state's nonlocal term needs its spectrum: diagnostics-only pencil pass
+        int nb = 0;
+        int rc = launch_pencil_pass<T>(ctx, fin, 0, 1, &nb);
+        if (rc != XPFC_OK) return rc;
+        XPFC_LAUNCH(ctx, launch_finalize(NQ_PEN, ctx->partials, nb, ctx->slots + 8 * slot[fin] + 4, ctx->stream));
+    }
+    if (ns > 0)
+        XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->hslots, ctx->slots, sizeof(double) * 8 * ns, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    ctx->iteration = fin;
+    ctx->diag_pending = true;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_collect(xpfc_ctx *ctx, xpfc_diag *out, int cap, int *count) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (count) *count = 0;
+    if (!ctx->diag_pending) return XPFC_OK;
+    const xpfc_params &p = ctx->p;
+    const double N = (double)ctx->ncells;
+    int produced = 0;
+    bool nonfinite = false;
+    for (size_t s = 0; s < ctx->diag_its.size(); s++) {
+        const long long i = ctx->diag_its[s];
+        const double *v = ctx->hslots + 8 * s;
+        xpfc_diag d;
+        d.iteration = i;
+        d.has = 0;
+        d.F = d.mean = d.rms = NAN;
+        if (diag_wantF(ctx, i)) {
+            d.F = p.ff_factor * (0.5 * v[1] - (p.a / 3.0) * v[2] + (p.b / 4.0) * v[3] - 0.5 * v[4] / N);
+            d.mean = v[0] / N;
+            d.has |= 1;
+            if (!std::isfinite(d.F) || !std::isfinite(d.mean)) nonfinite = true;
+        }
+        if (diag_wantR(ctx, i)) {
+            d.rms = std::sqrt(v[5]) / N;
+            d.has |= 2;
+        }
+        if (!d.has) continue;
+        if (out && produced < cap) out[produced] = d;
+        produced++;
+    }
+    if (count) *count = (!out || produced < cap) ? produced : cap;
+    if (nonfinite) return fail(ctx, XPFC_ENONFINITE, "free energy or mean is not finite");
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_step(xpfc_ctx *ctx, long long nsteps, xpfc_diag *out, int cap, int *count) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    if (!ctx->initialized) return fail(ctx, XPFC_ESTATE, "xpfc_step before xpfc_initialize");
+    if (nsteps < 0) return fail(ctx, XPFC_EINVAL, "nsteps < 0");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    int rc = ctx->esz == 4 ? fused_enqueue<float>(ctx, nsteps, true) : fused_enqueue<double>(ctx, nsteps, true);
+    if (rc != XPFC_OK) return rc;
+    return xpfc_collect(ctx, out, cap, count);
+}
+
+extern "C" int xpfc_step_async(xpfc_ctx *ctx, long long nsteps) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    if (!ctx->initialized) return fail(ctx, XPFC_ESTATE, "xpfc_step_async before xpfc_initialize");
+    if (nsteps < 0) return fail(ctx, XPFC_EINVAL, "nsteps < 0");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    return ctx->esz == 4 ? fused_enqueue<float>(ctx, nsteps, false) : fused_enqueue<double>(ctx, nsteps, false);
+}
+
+extern "C" int xpfc_set_profiling(xpfc_ctx *ctx, int enable) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    drain_profile(ctx);
+    ctx->profiling = enable != 0;
+    for (int i = 0; i < 8; i++) {
+        ctx->prof_ms[i] = 0.0;
+        ctx->prof_n[i] = 0;
+    }
+    if (ctx->profiling && ctx->ev_pool.empty()) {
+        ctx->ev_pool.resize(16384);
+        for (auto &e : ctx->ev_pool) XPFC_CUDA(ctx, cudaEventCreate(&e));
+    }
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_get_profile(xpfc_ctx *ctx, int pass, double *ms, long long *launches) {
+    if (!ctx || pass < 0 || pass >= 8) return fail(ctx, XPFC_EINVAL, "bad argument");
+    drain_profile(ctx);
+    if (ms) *ms = ctx->prof_ms[pass];
+    if (launches) *launches = ctx->prof_n[pass];
+    return XPFC_OK;
+}
+
+template <typename T>
+static int field_to_X(xpfc_ctx *ctx) {
+    const bool dbl = sizeof(T) == 8;
+    if (!ctx->X) XPFC_CUDA(ctx, cudaMalloc(&ctx->X, ctx->esz * (size_t)ctx->ncells));
+    void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl);
+    if (!tw0 || !tw2) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+    RowArgs ra{};
+    ra.nrows = (long long)ctx->n1 * ctx->n2;
+    ra.out = ctx->X;
+    if (ctx->three_d) {
+        void *tw1 = twiddle(ctx, ctx->n1, dbl);
+        ColArgs cy{};
+        cy.in = ctx->S;
+        cy.out = ctx->X;
+        cy.es = ctx->L0;
+        cy.ostride = (long long)ctx->n1 * ctx->L0;
+        cy.scale = 1.0;
+        cy.ncols = ctx->L0;
+        XPFC_LAUNCH(ctx, launch_col<T>(1, ctx->n1, cy, ctx->n2, tw1, ctx->stream));
+        ra.in = ctx->X;
+        ra.scale = 1.0 / ((double)ctx->n0 * ctx->n1);
+    } else {
+        ra.in = ctx->S;
+        ra.scale = 1.0 / (double)ctx->n0;
+    }
+    XPFC_LAUNCH(ctx, launch_row<T>(ROW_INV, ctx->L0, ra, tw0, tw2, ctx->stream, nullptr));
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_get_field(xpfc_ctx *ctx, double *host_psi) {
+    if (!ctx || !host_psi) return fail(ctx, XPFC_EINVAL, "null argument");
+    if (!ctx->initialized) return fail(ctx, XPFC_ESTATE, "no field before xpfc_initialize");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    int rc = ctx->esz == 4 ? field_to_X<float>(ctx) : field_to_X<double>(ctx);
+    if (rc != XPFC_OK) return rc;
+    const size_t n = (size_t)ctx->ncells;
+    rc = host_stage(ctx, ctx->esz * n);
+    if (rc != XPFC_OK) return rc;
+    XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->hstage, ctx->X, ctx->esz * n, cudaMemcpyDeviceToHost, ctx->stream));
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->esz == 4) {
+        const float *f = (const float *)ctx->hstage;
+        for (size_t i = 0; i < n; i++) host_psi[i] = (double)f[i];
+    } else {
+        memcpy(host_psi, ctx->hstage, sizeof(double) * n);
+    }
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_get_field_device_f32(xpfc_ctx *ctx, float *dev_out) {
+    if (!ctx || !dev_out) return fail(ctx, XPFC_EINVAL, "null argument");
+    if (!ctx->initialized) return fail(ctx, XPFC_ESTATE, "no field before xpfc_initialize");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    int rc = ctx->esz == 4 ? field_to_X<float>(ctx) : field_to_X<double>(ctx);
+    if (rc != XPFC_OK) return rc;
+    const long long n = ctx->ncells;
+    if (ctx->esz == 4)
+        XPFC_CUDA(ctx, cudaMemcpyAsync(dev_out, ctx->X, sizeof(float) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    else
+        XPFC_LAUNCH(ctx, launch_convert_d2f((const double *)ctx->X, dev_out, n, ctx->stream));
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return XPFC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// staged API (FP64, reference semantics)
+// ---------------------------------------------------------------------------
+#define XPFC_BUF(ctx, var, id)                                                           \
+    double *var = staged_buf(ctx, id);                                                   \
+    if (!var) return fail(ctx, (id) < 0 || (id) >= XPFC_NBUF ? XPFC_EINVAL : XPFC_ENOMEM, \
+                          "bad or unallocatable buffer id " + std::to_string(id))
+
+static int sync_or_fail(xpfc_ctx *ctx) {
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_upload(xpfc_ctx *ctx, int buf, const double *host) {
+    if (!ctx || !host) return fail(ctx, XPFC_EINVAL, "null argument");
+    XPFC_BUF(ctx, d, buf);
+    XPFC_CUDA(ctx, cudaMemcpyAsync(d, host, sizeof(double) * ctx->ncells, cudaMemcpyHostToDevice, ctx->stream));
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_download(xpfc_ctx *ctx, int buf, double *host) {
+    if (!ctx || !host) return fail(ctx, XPFC_EINVAL, "null argument");
+    XPFC_BUF(ctx, d, buf);
+    XPFC_CUDA(ctx, cudaMemcpyAsync(host, d, sizeof(double) * ctx->ncells, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_download_spectrum(xpfc_ctx *ctx, int buf, double *host_half) {
+    if (!ctx || !host_half) return fail(ctx, XPFC_EINVAL, "null argument");
+    XPFC_BUF(ctx, d, buf);
+    std::vector<double> pk(ctx->ncells);
+    XPFC_CUDA(ctx, cudaMemcpyAsync(pk.data(), d, sizeof(double) * ctx->ncells, cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = sync_or_fail(ctx);
+    if (rc != XPFC_OK) return rc;
+    const int L0 = ctx->L0, n1 = ctx->n1, n2 = ctx->n2, H = L0 + 1;
+    for (int i2 = 0; i2 < n2; i2++)
+        for (int i1 = 0; i1 < n1; i1++) {
+            const size_t row = ((size_t)i2 * n1 + i1);
+            const double *pr = pk.data() + 2 * row * L0;
+            double *o = host_half + 2 * row * H;
+            for (int k = 1; k < L0; k++) {
+                o[2 * k] = pr[2 * k];
+                o[2 * k + 1] = pr[2 * k + 1];
+            }
+            const int j1 = (n1 - i1) % n1, j2 = (n2 - i2) % n2;
+            const double *pm = pk.data() + 2 * ((size_t)j2 * n1 + j1) * L0;
+            const double Pr = pr[0], Pi = pr[1], Mr = pm[0], Mi = pm[1];
+            // X0 = (P + conj Pm)/2, XN = -i (P - conj Pm)/2
+            o[0] = 0.5 * (Pr + Mr);
+            o[1] = 0.5 * (Pi - Mi);
+            o[2 * L0] = 0.5 * (Pi + Mi);
+            o[2 * L0 + 1] = -0.5 * (Pr - Mr);
+        }
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_copy(xpfc_ctx *ctx, int src, int dst) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    XPFC_BUF(ctx, s, src);
+    XPFC_BUF(ctx, d, dst);
+    if (s != d)
+        XPFC_CUDA(ctx, cudaMemcpyAsync(d, s, sizeof(double) * ctx->ncells, cudaMemcpyDeviceToDevice, ctx->stream));
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_fft(xpfc_ctx *ctx, int buf, int direction) {
+    if (!ctx || (direction != XPFC_FORWARD && direction != XPFC_INVERSE)) return fail(ctx, XPFC_EINVAL, "bad argument");
+    XPFC_BUF(ctx, d, buf);
+    int rc = fft_full<double>(ctx, d, direction);
+    if (rc != XPFC_OK) return rc;
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_power_functions(xpfc_ctx *ctx, int in, int out, int pw) {
+    if (!ctx || pw < 2 || pw > 4) return fail(ctx, XPFC_EINVAL, "power must be 2, 3 or 4");
+    XPFC_BUF(ctx, s, in);
+    XPFC_BUF(ctx, d, out);
+    XPFC_LAUNCH(ctx, launch_power<double>(s, d, ctx->ncells, pw, ctx->p.ref_compat, ctx->stream));
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_scaling_step(xpfc_ctx *ctx, int buf) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    XPFC_BUF(ctx, d, buf);
+    XPFC_LAUNCH(ctx, launch_scale<double>(d, ctx->ncells, 1.0 / (double)ctx->ncells, ctx->stream));
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_copy_matrix(xpfc_ctx *ctx, int in, int out) {
+    // copy_matrix.cu:34-49 keeps the real part; the real buffers here hold only it
+    return xpfc_copy(ctx, in, out);
+}
+
+static int kspace_op(xpfc_ctx *ctx, int op, int out, int a1, int a2, int a3, int a4) {
+    if (out == a1 || out == a2 || out == a3 || out == a4)
+        return fail(ctx, XPFC_EINVAL, "k-space stages need an output buffer distinct from their inputs");
+    XPFC_BUF(ctx, o, out);
+    XPFC_BUF(ctx, x1, a1);
+    double *x2 = a2 >= 0 ? staged_buf(ctx, a2) : nullptr;
+    double *x3 = a3 >= 0 ? staged_buf(ctx, a3) : nullptr;
+    double *x4 = a4 >= 0 ? staged_buf(ctx, a4) : nullptr;
+    if ((a2 >= 0 && !x2) || (a3 >= 0 && !x3) || (a4 >= 0 && !x4)) return fail(ctx, XPFC_EINVAL, "bad buffer id");
+    KSpace ks = make_kspace(ctx, true);
+    XPFC_LAUNCH(ctx, launch_kspace<double>(op, ks, ctx->p.a, ctx->p.b, o, x1, x2, x3, x4, ctx->stream));
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_convolve_fields(xpfc_ctx *ctx, int psi_k, int out) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    return kspace_op(ctx, KOP_CONVOLVE, out, psi_k, -1, -1, -1);
+}
+
+extern "C" int xpfc_euler_step(xpfc_ctx *ctx, int n, int psi_kp1, int psi_k, int psi2_k, int psi3_k) {
+    (void)n;
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    return kspace_op(ctx, KOP_EULER, psi_kp1, psi_k, psi2_k, psi3_k, -1);
+}
+
+static int reduce_sum(xpfc_ctx *ctx, const double *psi, const double *p2, const double *p3, const double *p4,
+                      const double *convl, int square, double *result) {
+    int nb = 0;
+    XPFC_LAUNCH(ctx, launch_density<double>(psi, p2, p3, p4, convl, ctx->ncells, ctx->p.a, ctx->p.b, square,
+                                            ctx->p.ref_compat, ctx->partials, ctx->stream, &nb));
+    XPFC_LAUNCH(ctx, launch_finalize(1, ctx->partials, nb, ctx->init_red + 4, ctx->stream));
+    XPFC_CUDA(ctx, cudaMemcpyAsync(result, ctx->init_red + 4, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_or_fail(ctx);
+}
+
+extern "C" int xpfc_FE_calc(xpfc_ctx *ctx, int n, int psi, int psi2, int psi3, int psi4, int convl_r, double *F) {
+    (void)n;
+    if (!ctx || !F) return fail(ctx, XPFC_EINVAL, "null argument");
+    XPFC_BUF(ctx, a, psi);
+    XPFC_BUF(ctx, b2, psi2);
+    XPFC_BUF(ctx, b3, psi3);
+    XPFC_BUF(ctx, b4, psi4);
+    XPFC_BUF(ctx, c, convl_r);
+    double s = 0.0;
+    int rc = reduce_sum(ctx, a, b2, b3, b4, c, 0, &s);
+    if (rc != XPFC_OK) return rc;
+    *F = s * ctx->p.ff_factor;
+    if (!std::isfinite(*F)) return fail(ctx, XPFC_ENONFINITE, "free energy is not finite");
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_Avg_calc(xpfc_ctx *ctx, int buf, double *mean) {
+    if (!ctx || !mean) return fail(ctx, XPFC_EINVAL, "null argument");
+    XPFC_BUF(ctx, a, buf);
+    double s = 0.0;
+    int rc = reduce_sum(ctx, a, nullptr, nullptr, nullptr, nullptr, 0, &s);
+    if (rc != XPFC_OK) return rc;
+    *mean = s / (double)ctx->ncells;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_sse_calculation(xpfc_ctx *ctx, int n, int psi_kp1, int psi_k, int psi2_k, int psi3_k,
+                                    double *rms) {
+    (void)n;
+    if (!ctx || !rms) return fail(ctx, XPFC_EINVAL, "null argument");
+    int rc = kspace_op(ctx, KOP_RESIDUAL, XPFC_BUF_RES, psi_kp1, psi_k, psi2_k, psi3_k);
+    if (rc != XPFC_OK) return rc;
+    double *res = staged_buf(ctx, XPFC_BUF_RES);
+    rc = fft_full<double>(ctx, res, XPFC_INVERSE);
+    if (rc != XPFC_OK) return rc;
+    XPFC_LAUNCH(ctx, launch_scale<double>(res, ctx->ncells, 1.0 / (double)ctx->ncells, ctx->stream));
+    double s = 0.0;
+    rc = reduce_sum(ctx, res, nullptr, nullptr, nullptr, nullptr, 1, &s);
+    if (rc != XPFC_OK) return rc;
+    *rms = std::sqrt(s / (double)ctx->ncells);   // sum_reduction.cu:77
+    return XPFC_OK;
+}

@@ -1,0 +1,633 @@
+// xpfc_kernels.cuh -- the passes of the XPFC step on sm_103a.
+//
+// Device layout (n0 = fastest axis, the real-FFT axis; n2 = 1 in 2-D):
+//   real field      T      [n2][n1][n0]
+//   packed spectrum cplx<T>[n2][n1][n0/2]   (same bytes as the real field)
+// Row transform of a real row x (length n0 = 2 L): z[m] = x[2m] + i x[2m+1],
+// Z = FFT_L(z), X[k] = E[k] + W_{2L}^k O[k] with E = (Z[k] + conj Z[L-k])/2,
+// O = -i (Z[k] - conj Z[L-k])/2; slot 0 stores X[0] + i X[L] (both real).
+// The other axes are full complex FFTs of the packed rows, so after them
+// slot 0 holds X0 + i XN, X0 and XN the Hermitian (k1,k2)-planes of kx = 0 and
+// kx = n0/2; they separate with the mirror (-k1,-k2):
+//   X0 = (P + conj Pm)/2,  XN = (P - conj Pm)/(2i).
+#pragma once
+#include "fft_core.cuh"
+
+namespace xpfc {
+
+constexpr int NQ_ROW = 4;   // sum x, sum P2(x), sum P3(x), sum P4(x)
+constexpr int NQ_PEN = 2;   // sum w c2 |X|^2, sum w |res|^2
+
+// ---------------------------------------------------------------------------
+// shapes chosen at compile time from the line length
+// ---------------------------------------------------------------------------
+template <int L> struct RowShape {
+    static constexpr int TPL = L >= 32 ? L / 16 : (L >= 16 ? 2 : 1);
+    static constexpr int ROWS = (TPL >= 128) ? 1 : (128 / TPL > 32 ? 32 : 128 / TPL);
+    static constexpr int THREADS = ROWS * TPL;
+};
+
+template <typename T, int L> struct ColShape {
+    // tile width: keep the [L][TX] tile near 64 KB
+    static constexpr int BYTES = 65536;
+    static constexpr int TXc = BYTES / (L * (int)sizeof(cplx<T>));
+    static constexpr int TX = TXc >= 16 ? 16 : TXc >= 8 ? 8 : TXc >= 4 ? 4 : TXc >= 2 ? 2 : 1;
+    static constexpr int TPLc = L >= 32 ? L / 16 : 1;
+    static constexpr int TPL = (TPLc * TX > 1024) ? 1024 / TX : TPLc;
+    static constexpr int THREADS = TX * TPL;
+};
+
+template <typename T, int L, int NG> struct PenShape {
+    // 2*NG [L][TX] tiles (S and W; pencil and, in 3-D, its mirror) near 128 KB
+    static constexpr int BYTES = 131072;
+    static constexpr int TXc = BYTES / (2 * NG * L * (int)sizeof(cplx<T>));
+    static constexpr int TX = TXc >= 16 ? 16 : TXc >= 8 ? 8 : TXc >= 4 ? 4 : TXc >= 2 ? 2 : 1;
+    static constexpr int TPLc = L >= 32 ? L / 16 : 1;
+    static constexpr int TPL = (2 * NG * TX * TPLc > 1024) ? 1024 / (2 * NG * TX) : TPLc;
+    static constexpr int THREADS = 2 * NG * TX * TPL;
+};
+
+// ---------------------------------------------------------------------------
+// real-space op
+// ---------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T powi(T x, int p, int ref_compat) {
+    if (ref_compat) return (T)powf((float)x, (float)p);   // power_functions.cu:47
+    if (p == 2) return x * x;
+    if (p == 3) return x * x * x;
+    T s = x * x;
+    return s * s;
+}
+
+struct RowArgs {
+    const void *in;
+    void *out;
+    void *real_out;       // optional copy of the real field (type T), may be null
+    long long nrows;
+    double a, b;
+    double scale;         // multiplies the inverse-transform output
+    double *partials;     // [gridDim.x][NQ_ROW] when want_red
+    int want_red;
+    int ref_compat;
+};
+
+enum { ROW_FWD = 0, ROW_INV = 1, ROW_FUSED = 2, ROW_NL_FWD = 3 };
+
+// C2R pre-processing of one row (thread t of TPL handles pairs k, L-k)
+template <typename T, int L, int TPL>
+__device__ __forceinline__ void row_unpack(cplx<T> *line, int t, const cplx<T> *__restrict__ tw2) {
+    using I = LineIdx<T, 1>;
+    for (int k = t; k <= L / 2; k += TPL) {
+        if (k == 0) {
+            cplx<T> p = line[I::at(0)];
+            // Z0 = (X0 + XL) + i (X0 - XL)
+            line[I::at(0)] = mk<T>(p.x + p.y, p.x - p.y);
+            continue;
+        }
+        const int kk = L - k;
+        cplx<T> xk = line[I::at(k)], xc = line[I::at(kk)];
+        // Z[k] = (Xk + conj X[L-k]) + i (Xk - conj X[L-k]) W^{-k}
+        cplx<T> e = cadd(xk, cconj(xc));
+        cplx<T> o = cmulc(csub(xk, cconj(xc)), tw2[k]);
+        cplx<T> zk = cadd(e, cmuli<1>(o));
+        if (kk != k) {
+            // Z[L-k] from X[L-k] and conj X[k]; W_{2L}^{-(L-k)} = -W_{2L}^{k}
+            cplx<T> e2 = cadd(xc, cconj(xk));
+            cplx<T> o2 = cmul(csub(xc, cconj(xk)), tw2[k]);
+            o2 = mk<T>(-o2.x, -o2.y);
+            line[I::at(kk)] = cadd(e2, cmuli<1>(o2));
+        }
+        line[I::at(k)] = zk;
+    }
+}
+
+// R2C post-processing of one row, packing X[L] into slot 0
+template <typename T, int L, int TPL>
+__device__ __forceinline__ void row_pack(cplx<T> *line, int t, const cplx<T> *__restrict__ tw2) {
+    using I = LineIdx<T, 1>;
+    const T h = (T)0.5;
+    for (int k = t; k <= L / 2; k += TPL) {
+        if (k == 0) {
+            cplx<T> z = line[I::at(0)];
+            line[I::at(0)] = mk<T>(z.x + z.y, z.x - z.y);
+            continue;
+        }
+        const int kk = L - k;
+        cplx<T> zk = line[I::at(k)], zc = line[I::at(kk)];
+        // X[k] = (Zk + conj Zc)/2 - i W^k (Zk - conj Zc)/2
+        cplx<T> e = cadd(zk, cconj(zc));
+        cplx<T> o = cmul(csub(zk, cconj(zc)), tw2[k]);
+        cplx<T> xk = cscale(csub(e, cmuli<1>(o)), h);
+        if (kk != k) {
+            // W_{2L}^{L-k} = -conj(W_{2L}^k)
+            cplx<T> e2 = cadd(zc, cconj(zk));
+            cplx<T> o2 = cmulc(csub(zc, cconj(zk)), tw2[k]);
+            o2 = mk<T>(-o2.x, -o2.y);
+            line[I::at(kk)] = cscale(csub(e2, cmuli<1>(o2)), h);
+        }
+        line[I::at(k)] = xk;
+    }
+}
+
+// Row pass over rows of n0 = 2L reals.  One block handles ROWS rows.
+template <typename T, int L, int MODE>
+__global__ void __launch_bounds__(RowShape<L>::THREADS)
+row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restrict__ tw2L) {
+    using S = RowShape<L>;
+    using I = LineIdx<T, 1>;
+    constexpr int SPAN = I::span(L);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);          // L
+    cplx<T> *stw2 = stw + L;                                        // L
+    cplx<T> *lines = stw2 + L;                                      // ROWS * SPAN
+    double *sred = reinterpret_cast<double *>(lines + S::ROWS * SPAN);
+
+    const int tid = threadIdx.x;
+    for (int i = tid; i < L; i += S::THREADS) {
+        stw[i] = twL[i];
+        stw2[i] = tw2L[i];
+    }
+    const long long row0 = (long long)blockIdx.x * S::ROWS;
+    const int nvalid = (int)min((long long)S::ROWS, args.nrows - row0);
+    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + row0 * L;
+    for (int e = tid; e < nvalid * L; e += S::THREADS) {
+        const int r = e / L, c = e - r * L;
+        lines[r * SPAN + I::at(c)] = gin[e];
+    }
+    __syncthreads();
+
+    const int r = tid / S::TPL, t = tid - r * S::TPL;
+    cplx<T> *line = lines + r * SPAN;
+
+    if (MODE == ROW_INV || MODE == ROW_FUSED) {
+        row_unpack<T, L, S::TPL>(line, t, stw2);
+        __syncthreads();
+        line_fft<T, L, +1, S::TPL, 1>(line, t, stw);
+    }
+
+    if (MODE == ROW_INV) {
+        const T sc = (T)args.scale;
+        for (int m = t; m < L; m += S::TPL) line[I::at(m)] = cscale(line[I::at(m)], sc);
+        __syncthreads();
+    } else if (MODE == ROW_FUSED || MODE == ROW_NL_FWD) {
+        // real-space op: n -> N(n) = -a n^2 + b n^3, with FP64 sums
+        double v[NQ_ROW] = {0.0, 0.0, 0.0, 0.0};
+        const T sc = (T)args.scale;
+        const T a = (T)args.a, b = (T)args.b;
+        const bool valid = r < nvalid;
+        T *rout = args.real_out ? reinterpret_cast<T *>(args.real_out) + (row0 + r) * (2 * L) : nullptr;
+        for (int m = t; m < L; m += S::TPL) {
+            cplx<T> z = line[I::at(m)];
+            T x0 = z.x, x1 = z.y;
+            if (MODE == ROW_FUSED) { x0 *= sc; x1 *= sc; }
+            if (rout && valid) { rout[2 * m] = x0; rout[2 * m + 1] = x1; }
+            T p20 = powi(x0, 2, args.ref_compat), p21 = powi(x1, 2, args.ref_compat);
+            T p30 = powi(x0, 3, args.ref_compat), p31 = powi(x1, 3, args.ref_compat);
+            if (args.want_red && valid) {
+                v[0] += (double)x0 + (double)x1;
+                v[1] += (double)p20 + (double)p21;
+                v[2] += (double)p30 + (double)p31;
+                v[3] += (double)powi(x0, 4, args.ref_compat) + (double)powi(x1, 4, args.ref_compat);
+            }
+            line[I::at(m)] = mk<T>(-a * p20 + b * p30, -a * p21 + b * p31);
+        }
+        if (args.want_red) block_reduce_store<NQ_ROW>(v, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
+        __syncthreads();
+    }
+
+    if (MODE != ROW_INV) {
+        line_fft<T, L, -1, S::TPL, 1>(line, t, stw);
+        row_pack<T, L, S::TPL>(line, t, stw2);
+        __syncthreads();
+    }
+
+    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + row0 * L;
+    for (int e = tid; e < nvalid * L; e += S::THREADS) {
+        const int rr = e / L, c = e - rr * L;
+        gout[e] = lines[rr * SPAN + I::at(c)];
+    }
+}
+
+template <typename T, int L> constexpr size_t row_smem_bytes() {
+    using S = RowShape<L>;
+    return sizeof(cplx<T>) * (2 * L + S::ROWS * LineIdx<T, 1>::span(L)) + sizeof(double) * 32 * NQ_ROW;
+}
+
+// ---------------------------------------------------------------------------
+// Column pass: C2C FFT along a strided axis for tiles of TX adjacent columns.
+// Block (x = column tile, y = outer index); element e of column c of the tile
+// lives at base + e*es + c with base = x*TX + y*ostride.
+// ---------------------------------------------------------------------------
+struct ColArgs {
+    const void *in;
+    void *out;
+    long long es;         // element stride (complex units)
+    long long ostride;    // stride per blockIdx.y
+    double scale;
+    int ncols;            // columns in a row (n0/2); the last tile may be partial
+};
+
+template <typename T, int L, int DIR>
+__global__ void __launch_bounds__(ColShape<T, L>::THREADS)
+col_kernel(ColArgs args, const cplx<T> *__restrict__ twL) {
+    using S = ColShape<T, L>;
+    constexpr int TX = S::TX;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *tile = stw + L;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < L; i += S::THREADS) stw[i] = twL[i];
+    const long long base = (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride;
+    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + base;
+    const int c = tid % TX, t = tid / TX;
+    const bool cvalid = (int)blockIdx.x * TX + c < args.ncols;
+    if (cvalid)
+        for (int e = t; e < L; e += S::TPL) tile[e * TX + c] = gin[e * args.es + c];
+    __syncthreads();
+    line_fft<T, L, DIR, S::TPL, TX>(tile + c, t, stw);
+    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + base;
+    const T sc = (T)args.scale;
+    if (!cvalid) return;
+    if (args.scale != 1.0)
+        for (int e = t; e < L; e += S::TPL) gout[e * args.es + c] = cscale(tile[e * TX + c], sc);
+    else
+        for (int e = t; e < L; e += S::TPL) gout[e * args.es + c] = tile[e * TX + c];
+}
+
+template <typename T, int L> constexpr size_t col_smem_bytes() {
+    using S = ColShape<T, L>;
+    return sizeof(cplx<T>) * (L + L * S::TX);
+}
+
+// ---------------------------------------------------------------------------
+// k-space coefficients
+// ---------------------------------------------------------------------------
+struct KSpace {
+    int n0, n1, n2;                 // grid (n0 real axis)
+    double dk0sq, dk1sq, dk2sq;     // (2 pi/L_d)^2
+    const void *table;              // per shell m: {A, B, c2, k2} in T, or null
+    int mmax;
+    // on-the-fly coefficients (no table)
+    double dt, Mo, Mo_res, eps;
+    int npeaks, envelope;
+    double pk_k[8], pk_inv2a2[8], pk_dw[8];
+    // noise
+    int noise_on;
+    double noise_scale;             // amp * sqrt(cells)
+    unsigned long long noise_seed;
+    long long step;
+};
+
+template <typename T> struct Coef { T A, B, c2, k2; };
+
+__device__ __forceinline__ int signed_idx(int i, int n) { return 2 * i <= n ? i : i - n; }
+
+template <typename T>
+__device__ __forceinline__ Coef<T> kcoef(const KSpace &ks, int i0, int i1, int i2) {
+    const int s1 = signed_idx(i1, ks.n1), s2 = signed_idx(i2, ks.n2);
+    Coef<T> r;
+    if (ks.table) {
+        const int m = i0 * i0 + s1 * s1 + s2 * s2;
+        const T *e = reinterpret_cast<const T *>(ks.table) + 4 * (size_t)m;
+        r.A = e[0]; r.B = e[1]; r.c2 = e[2]; r.k2 = e[3];
+        return r;
+    }
+    const T k2 = (T)ks.dk0sq * (T)(i0 * i0) + (T)ks.dk1sq * (T)(s1 * s1) + (T)ks.dk2sq * (T)(s2 * s2);
+    const T kk = sqrt(k2);
+    T c2 = (T)0;
+    for (int p = 0; p < ks.npeaks; p++) {
+        const T d = kk - (T)ks.pk_k[p];
+        const T v = (T)ks.pk_dw[p] * exp(-(d * d) * (T)ks.pk_inv2a2[p]);
+        c2 = ks.envelope == 0 ? c2 + v : (p == 0 || v > c2 ? v : c2);
+    }
+    const T dt = (T)ks.dt, Mo = (T)ks.Mo;
+    const T den = ((T)1 + k2 * dt * Mo * ((T)1 - (T)ks.eps) - k2 * Mo * dt * c2);
+    r.A = (T)1 / den;
+    r.B = -(k2 * Mo * dt) / den;
+    r.c2 = c2;
+    r.k2 = k2;
+    return r;
+}
+
+// conserved noise xi_k = amp sqrt(cells) |k| g_k at full-grid mode (i0,i1,i2),
+// i0 in [0, n0/2]; Hermitian pairing as the oracle defines it
+template <typename T>
+__device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, int i0, int i1, int i2, T k2) {
+    const int j1 = (ks.n1 - i1) % ks.n1, j2 = (ks.n2 - i2) % ks.n2;
+    const bool edge = (i0 == 0) || (2 * i0 == ks.n0);
+    const bool selfc = edge && j1 == i1 && j2 == i2;
+    bool canon = true;
+    long long ci;
+    if (edge) {
+        const long long l = (long long)i2 * ks.n1 + i1, lm = (long long)j2 * ks.n1 + j1;
+        canon = l <= lm;
+        ci = canon ? l * ks.n0 + i0 : lm * ks.n0 + i0;
+    } else {
+        ci = ((long long)i2 * ks.n1 + i1) * ks.n0 + i0;
+    }
+    const unsigned long long stream = 1ull + (unsigned long long)ks.step;
+    uint4 o = philox4x32_10(make_uint4((uint32_t)ci, (uint32_t)((unsigned long long)ci >> 32), (uint32_t)stream,
+                                       (uint32_t)(stream >> 32)),
+                            make_uint2((uint32_t)ks.noise_seed, (uint32_t)(ks.noise_seed >> 32)));
+    T g0, g1;
+    if (sizeof(T) == 8) {
+        const double u1 = ((double)o.x + 1.0) * 2.3283064365386963e-10;
+        const double u2 = (double)o.y * 2.3283064365386963e-10;
+        const double rr = sqrt(-2.0 * log(u1));
+        double sn, cs;
+        sincospi(2.0 * u2, &sn, &cs);
+        g0 = (T)(rr * cs);
+        g1 = (T)(rr * sn);
+    } else {
+        const float u1 = ((float)o.x + 1.0f) * 2.3283064365386963e-10f;
+        const float u2 = (float)o.y * 2.3283064365386963e-10f;
+        const float rr = sqrtf(-2.0f * logf(u1));
+        float sn, cs;
+        sincospif(2.0f * u2, &sn, &cs);
+        g0 = (T)(rr * cs);
+        g1 = (T)(rr * sn);
+    }
+    const T amp = (T)ks.noise_scale * sqrt(k2);
+    if (selfc) return mk<T>(amp * g0, (T)0);
+    const T h = (T)0.70710678118654752440;
+    return mk<T>(amp * g0 * h, (canon ? amp : -amp) * g1 * h);
+}
+
+// ---------------------------------------------------------------------------
+// Pencil pass: along the last axis (z in 3-D, y in 2-D), fused
+//   forward FFT of S (state) and W (nonlinear term), the semi-implicit update,
+//   k-space diagnostics, inverse FFT of S.
+// 3-D: block (x = column tile, y = pair index p in [0, n1/2]) handles rows
+//   y1 = p and y2 = (n1 - p) % n1 of every z.  2-D: one group, y = pencil.
+// ---------------------------------------------------------------------------
+struct PenArgs {
+    void *S;
+    const void *W;
+    long long es;        // pencil element stride (complex)
+    long long gstride;   // stride of the paired axis (3-D: L0), 0 in 2-D
+    int three_d;
+    int L0;              // packed row length n0/2
+    double scale;        // folds the pencil-axis inverse normalisation
+    int update;          // 0: diagnostics only (no update, no store)
+    int want_red;
+    double *partials;
+    int pin;             // overwrite the k = 0 mode with pin_value (unscaled)
+    double pin_value;
+};
+
+template <typename T, int L, int NG>
+__global__ void __launch_bounds__(PenShape<T, L, NG>::THREADS)
+pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
+    using S = PenShape<T, L, NG>;
+    constexpr int TX = S::TX, TPL = S::TPL;
+    constexpr int TILE = L * TX;
+    constexpr int NT = 2 * NG;                      // tiles: [array][group]
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *tiles = stw + L;                        // [array 0..1][group 0..NG-1][L][TX]
+    double *sred = reinterpret_cast<double *>(tiles + NT * TILE);
+
+    const int tid = threadIdx.x;
+    for (int i = tid; i < L; i += S::THREADS) stw[i] = twL[i];
+
+    const int p = blockIdx.y;
+    int yg[2];
+    yg[0] = p;
+    yg[1] = (NG == 2) ? (ks.n1 - p) % ks.n1 : p;
+    const int G = (NG == 2 && yg[1] != yg[0]) ? 2 : 1;
+    const int kx0 = blockIdx.x * TX;
+    cplx<T> *gS = reinterpret_cast<cplx<T> *>(args.S);
+    const cplx<T> *gW = reinterpret_cast<const cplx<T> *>(args.W);
+
+    // load
+    {
+        const int c = tid % TX, rest = tid / TX;   // rest in [0, NT TPL)
+        if (kx0 + c < args.L0)
+            for (int idx = rest; idx < 2 * G * L; idx += NT * TPL) {
+                const int a = idx / (G * L), g = (idx / L) % G, e = idx % L;
+                const long long off = (long long)yg[g] * args.gstride + kx0 + c + (long long)e * args.es;
+                tiles[(a * NG + g) * TILE + e * TX + c] = (a == 0) ? gS[off] : gW[off];
+            }
+    }
+    __syncthreads();
+    // forward FFT of all (array, group, column) lines
+    {
+        const int c = tid % TX, t = (tid / TX) % TPL, ag = tid / (TX * TPL);
+        line_fft<T, L, -1, TPL, TX>(tiles + ag * TILE + c, t, stw);
+    }
+
+    // update: every thread handles modes (g, kz, c) in group-major order
+    double v[NQ_PEN] = {0.0, 0.0};
+    constexpr int PER = cdiv(NG * TILE, S::THREADS);
+    cplx<T> res[PER];
+    const T sc = (T)args.scale;
+    const int nh = args.L0;   // n0/2
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        const int idx = tid + q * S::THREADS;
+        if (idx >= G * TILE) continue;
+        const int g = idx / TILE, kz = (idx / TX) % L, c = idx % TX;
+        const int slot = kx0 + c;
+        if (slot >= args.L0) continue;
+        const int i1 = args.three_d ? yg[g] : kz;
+        const int i2 = args.three_d ? kz : 0;
+        const cplx<T> xs = tiles[(0 * NG + g) * TILE + kz * TX + c];
+        const cplx<T> xw = tiles[(1 * NG + g) * TILE + kz * TX + c];
+        cplx<T> out;
+        if (slot != 0) {
+            Coef<T> cf = kcoef<T>(ks, slot, i1, i2);
+            cplx<T> num = xs;
+            if (ks.noise_on) num = cadd(num, noise_at<T>(ks, slot, i1, i2, cf.k2));
+            cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
+            if (args.want_red) {
+                const double xr = xs.x, xi = xs.y;
+                const double k2 = cf.k2, c2 = cf.c2;
+                v[0] += 2.0 * c2 * (xr * xr + xi * xi);
+                const double rr = ((double)xn.x - xr) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xr + (double)xw.x);
+                const double ri = ((double)xn.y - xi) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xi + (double)xw.y);
+                v[1] += 2.0 * (rr * rr + ri * ri);
+            }
+            out = cscale(xn, sc);
+        } else {
+            // slot 0: separate the kx = 0 and kx = n0/2 planes with the mirror mode
+            const int gm = (G == 2) ? 1 - g : g;
+            const int kzm = (L - kz) % L;
+            const cplx<T> ps = tiles[(0 * NG + gm) * TILE + kzm * TX];
+            const cplx<T> pw = tiles[(1 * NG + gm) * TILE + kzm * TX];
+            const T h = (T)0.5;
+            // X0 = (P + conj Pm)/2, XN = (P - conj Pm)/(2i) = -i (P - conj Pm)/2
+            const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
+            const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
+            const Coef<T> c0 = kcoef<T>(ks, 0, i1, i2), cN = kcoef<T>(ks, nh, i1, i2);
+            cplx<T> num0 = s0, numN = sN;
+            if (ks.noise_on) {
+                num0 = cadd(num0, noise_at<T>(ks, 0, i1, i2, c0.k2));
+                numN = cadd(numN, noise_at<T>(ks, nh, i1, i2, cN.k2));
+            }
+            cplx<T> x0n = mk<T>(c0.A * num0.x + c0.B * w0.x, c0.A * num0.y + c0.B * w0.y);
+            cplx<T> xNn = mk<T>(cN.A * numN.x + cN.B * wN.x, cN.A * numN.y + cN.B * wN.y);
+            if (args.pin && i1 == 0 && i2 == 0) x0n = mk<T>((T)args.pin_value, (T)0);
+            if (args.want_red) {
+                const double k20 = c0.k2, c20 = c0.c2, k2N = cN.k2, c2N = cN.c2;
+                v[0] += c20 * ((double)s0.x * s0.x + (double)s0.y * s0.y);
+                v[0] += c2N * ((double)sN.x * sN.x + (double)sN.y * sN.y);
+                double rr = ((double)x0n.x - s0.x) / ks.dt + ks.Mo_res * k20 * ((1.0 - c20) * s0.x + (double)w0.x);
+                double ri = ((double)x0n.y - s0.y) / ks.dt + ks.Mo_res * k20 * ((1.0 - c20) * s0.y + (double)w0.y);
+                v[1] += rr * rr + ri * ri;
+                rr = ((double)xNn.x - sN.x) / ks.dt + ks.Mo_res * k2N * ((1.0 - c2N) * sN.x + (double)wN.x);
+                ri = ((double)xNn.y - sN.y) / ks.dt + ks.Mo_res * k2N * ((1.0 - c2N) * sN.y + (double)wN.y);
+                v[1] += rr * rr + ri * ri;
+            }
+            // repack P = X0 + i XN
+            out = cscale(cadd(x0n, cmuli<1>(xNn)), sc);
+        }
+        res[q] = out;
+    }
+    if (args.want_red)
+        block_reduce_store<NQ_PEN>(v, args.partials + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * NQ_PEN, sred);
+    if (!args.update) return;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        const int idx = tid + q * S::THREADS;
+        if (idx >= G * TILE) continue;
+        const int g = idx / TILE, kz = (idx / TX) % L, c = idx % TX;
+        if (kx0 + c >= args.L0) continue;
+        tiles[(0 * NG + g) * TILE + kz * TX + c] = res[q];
+    }
+    __syncthreads();
+    // inverse FFT of the state lines: NG TX lines, 2 TPL threads each
+    {
+        const int c = tid % TX, t = (tid / TX) % (2 * TPL), g = tid / (TX * 2 * TPL);
+        line_fft<T, L, +1, 2 * TPL, TX>(tiles + g * TILE + c, t, stw);
+    }
+    {
+        const int c = tid % TX, rest = tid / TX;
+        if (kx0 + c < args.L0)
+            for (int idx = rest; idx < G * L; idx += NT * TPL) {
+                const int g = idx / L, e = idx % L;
+                const long long off = (long long)yg[g] * args.gstride + kx0 + c + (long long)e * args.es;
+                gS[off] = tiles[g * TILE + e * TX + c];
+            }
+    }
+}
+
+template <typename T, int L, int NG> constexpr size_t pen_smem_bytes() {
+    using S = PenShape<T, L, NG>;
+    return sizeof(cplx<T>) * (L + 2 * NG * L * S::TX) + sizeof(double) * 32 * NQ_PEN;
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic final reduction of per-block partials: out[q] = sum_b part[b][q]
+// (one block; fixed order for a fixed partial count).
+// ---------------------------------------------------------------------------
+template <int NQ>
+__global__ void __launch_bounds__(256) finalize_kernel(const double *__restrict__ part, long long nparts,
+                                                       double *__restrict__ out) {
+    __shared__ double sred[32 * NQ];
+    double v[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) v[q] = 0.0;
+    for (long long b = threadIdx.x; b < nparts; b += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NQ; q++) v[q] += part[b * NQ + q];
+    block_reduce_store<NQ>(v, out, sred);
+}
+
+// ---------------------------------------------------------------------------
+// Staged API kernels (the reference's per-stage wrappers, FP64)
+// ---------------------------------------------------------------------------
+// power_functions.cu:34-53: out = in^p
+template <typename T>
+__global__ void power_kernel(const T *__restrict__ in, T *__restrict__ out, long long n, int p, int ref_compat) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = powi(in[i], p, ref_compat);
+}
+
+// scaling_step.cu:34-53: f *= s
+template <typename T>
+__global__ void scale_kernel(T *__restrict__ f, long long n, T s) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        f[i] *= s;
+}
+
+// element type conversion (upload to / download from the mixed state)
+template <typename A, typename B>
+__global__ void convert_kernel(const A *__restrict__ in, B *__restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (B)in[i];
+}
+
+// FE_calc.cu:54-68 density, summed per block: sum ff
+// Avg_calc: sum x (p2 == nullptr); squares (square = 1) for the residual RMS
+template <typename T>
+__global__ void __launch_bounds__(256) density_partials(const T *__restrict__ psi, const T *__restrict__ p2,
+                                                        const T *__restrict__ p3, const T *__restrict__ p4,
+                                                        const T *__restrict__ convl, long long n, double a, double b,
+                                                        int square, int ref_compat, double *__restrict__ partials) {
+    __shared__ double sred[32];
+    double v[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (p2)
+            v[0] += 0.5 * (double)p2[i] - (a / 3.0) * (double)p3[i] + (b / 4.0) * (double)p4[i] -
+                    0.5 * (double)psi[i] * (double)convl[i];
+        else if (square)
+            v[0] += (double)powi(psi[i], 2, ref_compat);
+        else
+            v[0] += (double)psi[i];
+    }
+    block_reduce_store<1>(v, partials + blockIdx.x, sred);
+}
+
+enum { KOP_EULER = 0, KOP_CONVOLVE = 1, KOP_RESIDUAL = 2 };
+
+// k-space pointwise op on packed spectra at full-grid mode (i0, i1, i2)
+template <typename T, int OP>
+__device__ __forceinline__ cplx<T> kop(const KSpace &ks, double a, double b, int i0, int i1, int i2, cplx<T> x1,
+                                        cplx<T> x2, cplx<T> x3, cplx<T> x4) {
+    const Coef<T> cf = kcoef<T>(ks, i0, i1, i2);
+    const T k2 = cf.k2, c2 = cf.c2, dt = (T)ks.dt, Mo = (T)ks.Mo;
+    if (OP == KOP_EULER) {
+        // euler_step.cu:50-59
+        const T ca = (T)a * k2 * Mo * dt, cb = (T)b * k2 * dt * Mo;
+        const T den = ((T)1 + k2 * dt * Mo * ((T)1 - (T)ks.eps) - k2 * Mo * dt * c2);
+        return mk<T>((x1.x + ca * x2.x - cb * x3.x) / den, (x1.y + ca * x2.y - cb * x3.y) / den);
+    } else if (OP == KOP_CONVOLVE) {
+        return cscale(x1, c2);   // convolve_fields.cu:41-42
+    } else {
+        // sse_calculation.cu:133-140 with x1 = psi_kp1, x2 = psi_k, x3 = psi2_k, x4 = psi3_k
+        const T Mr = (T)ks.Mo_res;
+        const T d2r = -Mr * k2 * (x2.x - (T)a * x3.x + (T)b * x4.x - c2 * x2.x);
+        const T d2i = -Mr * k2 * (x2.y - (T)a * x3.y + (T)b * x4.y - c2 * x2.y);
+        return mk<T>((x1.x - x2.x) / dt - d2r, (x1.y - x2.y) / dt - d2i);
+    }
+}
+
+template <typename T, int OP>
+__global__ void kspace_kernel(KSpace ks, double a, double b, cplx<T> *__restrict__ out, const cplx<T> *x1,
+                              const cplx<T> *x2, const cplx<T> *x3, const cplx<T> *x4) {
+    const int L0 = ks.n0 / 2;
+    const long long total = (long long)L0 * ks.n1 * ks.n2;
+    const cplx<T> z = mk<T>((T)0, (T)0);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int slot = (int)(i % L0);
+        const long long rest = i / L0;
+        const int i1 = (int)(rest % ks.n1), i2 = (int)(rest / ks.n1);
+        cplx<T> a1 = x1[i], a2 = x2 ? x2[i] : z, a3 = x3 ? x3[i] : z, a4 = x4 ? x4[i] : z;
+        if (slot != 0) {
+            out[i] = kop<T, OP>(ks, a, b, slot, i1, i2, a1, a2, a3, a4);
+            continue;
+        }
+        const int j1 = (ks.n1 - i1) % ks.n1, j2 = (ks.n2 - i2) % ks.n2;
+        const long long im = ((long long)j2 * ks.n1 + j1) * L0;
+        const cplx<T> m1 = x1[im], m2 = x2 ? x2[im] : z, m3 = x3 ? x3[im] : z, m4 = x4 ? x4[im] : z;
+        const T h = (T)0.5;
+        auto lo = [&](cplx<T> p, cplx<T> q) { return cscale(cadd(p, cconj(q)), h); };
+        auto hi = [&](cplx<T> p, cplx<T> q) { return cscale(cmuli<-1>(csub(p, cconj(q))), h); };
+        cplx<T> r0 = kop<T, OP>(ks, a, b, 0, i1, i2, lo(a1, m1), lo(a2, m2), lo(a3, m3), lo(a4, m4));
+        cplx<T> rN = kop<T, OP>(ks, a, b, ks.n0 / 2, i1, i2, hi(a1, m1), hi(a2, m2), hi(a3, m3), hi(a4, m4));
+        out[i] = cadd(r0, cmuli<1>(rN));
+    }
+}
+
+}  // namespace xpfc

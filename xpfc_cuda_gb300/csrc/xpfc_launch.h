@@ -1,0 +1,45 @@
+// xpfc_launch.h -- host-side launchers of the passes, one set per element
+// type (float: the mixed path; double: the plain FP64 path).  Each launcher
+// dispatches the runtime line length to its compile-time instance and
+// returns cudaErrorInvalidValue for a length that has none.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "xpfc_kernels.cuh"
+
+namespace xpfc {
+
+// Line lengths with compiled instances.
+bool row_supported(int L);          // L = n0/2
+bool col_supported(int L);          // n1 or n2 along a column pass
+bool pen_supported(int L, int ng);  // pencil length, groups (2: 3-D, 1: 2-D)
+
+template <typename T>
+cudaError_t launch_row(int mode, int L, const RowArgs &a, const void *twL, const void *tw2L, cudaStream_t s,
+                       int *nblocks);
+template <typename T>
+cudaError_t launch_col(int dir, int L, const ColArgs &a, int nouter, const void *twL, cudaStream_t s);
+template <typename T>
+cudaError_t launch_pencil(int L, int ng, const PenArgs &a, const KSpace &ks, int npairs, const void *twL,
+                          cudaStream_t s, int *nblocks);
+template <typename T>
+cudaError_t launch_kspace(int op, const KSpace &ks, double a, double b, void *out, const void *x1, const void *x2,
+                          const void *x3, const void *x4, cudaStream_t s);
+template <typename T>
+cudaError_t launch_power(const T *in, T *out, long long n, int p, int ref_compat, cudaStream_t s);
+template <typename T>
+cudaError_t launch_scale(T *f, long long n, double sc, cudaStream_t s);
+template <typename T>
+cudaError_t launch_density(const T *psi, const T *p2, const T *p3, const T *p4, const T *convl, long long n, double a,
+                           double b, int square, int ref_compat, double *partials, cudaStream_t s, int *nblocks);
+cudaError_t launch_convert_d2f(const double *in, float *out, long long n, cudaStream_t s);
+cudaError_t launch_convert_f2d(const float *in, double *out, long long n, cudaStream_t s);
+cudaError_t launch_finalize(int nq, const double *part, long long nparts, double *out, cudaStream_t s);
+
+// grid shapes the launchers use (for sizing the partials buffer)
+int row_rows(int L);
+template <typename T> int col_tx(int L);
+template <typename T> int pen_tx(int L, int ng);
+constexpr int DENSITY_BLOCKS = 1024;
+
+}  // namespace xpfc

@@ -1,0 +1,4 @@
+// float instances of the pass launchers (the mixed-precision path)
+#define XPFC_T float
+#define XPFC_COMMON
+#include "xpfc_launch.inc"
