@@ -469,7 +469,13 @@ double ox_ic_reference(double *psi, int Mx, int My, int Lx, int Ly, double psi0,
    Hermitian by construction: mode k with 0 < ix < nx/2 draws its own pair;
    its partner -k takes the conjugate; on the ix = 0 and ix = nx/2 planes the
    canonical member of {k,-k} is the one with the smaller (iz*ny+iy); a
-   self-conjugate mode takes a real draw.  Philox stream 1 + step. */
+   self-conjugate mode takes a real draw.
+   Draws: the slowest axis of the grid (z in 3-D, y in 2-D) is split in two
+   halves; a canonical mode with slow coordinate s uses Philox4x32-10 at
+   counter (index of the mode with s mod n/2, stream 1 + step), outputs 0,1 for
+   the lower half and 2,3 for the upper, each pair through Box-Muller
+   (u1 = (x+1) 2^-32, u2 = y 2^-32, r = sqrt(-2 ln u1), (r cos 2 pi u2,
+   r sin 2 pi u2)).  One Philox call so serves two modes. */
 void ox_noise_k(const ox_params *p, long step, double *noise_k) {
     const int nx = p->nx, ny = p->ny, nz = p->nz;
     const long cells = (long)nx * ny * nz;
@@ -481,6 +487,8 @@ void ox_noise_k(const ox_params *p, long step, double *noise_k) {
     ox_fft_freq(ny, p->Ly, ky);
     ox_fft_freq(nz, p->Lz, kz);
     if (nz == 1) kz[0] = 0.0;
+    const uint32_t key[2] = {(uint32_t)p->noise_seed, (uint32_t)(p->noise_seed >> 32)};
+    const uint64_t stream = 1 + (uint64_t)step;
 #pragma omp parallel for schedule(static)
     for (int iz = 0; iz < nz; iz++)
         for (int iy = 0; iy < ny; iy++)
@@ -491,9 +499,25 @@ void ox_noise_k(const ox_params *p, long step, double *noise_k) {
                 if (ix > 0 && 2 * ix < nx) canon = 1;
                 else if (2 * ix > nx) canon = 0;
                 else canon = ((long)iz * ny + iy) <= ((long)jz * ny + jy);
-                long ci = canon ? i : ((long)jz * ny + jy) * nx + jx;
-                double g0, g1;
-                ox_gauss_pair(p->noise_seed, 1 + (uint64_t)step, (uint64_t)ci, &g0, &g1);
+                int cx = canon ? ix : jx, cy = canon ? iy : jy, cz = canon ? iz : jz;
+                long ctr;
+                int upper;
+                if (nz > 1) {
+                    upper = 2 * cz >= nz;
+                    ctr = ((long)(cz % (nz / 2)) * ny + cy) * nx + cx;
+                } else {
+                    upper = 2 * cy >= ny;
+                    ctr = (long)(cy % (ny / 2)) * nx + cx;
+                }
+                const uint32_t c[4] = {(uint32_t)ctr, (uint32_t)((uint64_t)ctr >> 32), (uint32_t)stream,
+                                       (uint32_t)(stream >> 32)};
+                uint32_t o[4];
+                ox_philox4x32(c, key, o);
+                const uint32_t a = upper ? o[2] : o[0], b = upper ? o[3] : o[1];
+                const double u1 = ((double)a + 1.0) * 2.3283064365386963e-10;
+                const double u2 = (double)b * 2.3283064365386963e-10;
+                const double r = sqrt(-2.0 * log(u1));
+                const double g0 = r * cos(2.0 * M_PI * u2), g1 = r * sin(2.0 * M_PI * u2);
                 double kk = sqrt(kx[ix] * kx[ix] + ky[iy] * ky[iy] + kz[iz] * kz[iz]);
                 double re, im;
                 if (selfc) { re = g0; im = 0.0; }

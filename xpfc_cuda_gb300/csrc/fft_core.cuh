@@ -294,8 +294,10 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NQ], double *__re
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and Box-Muller.
 // ---------------------------------------------------------------------------
+// The round loop stays rolled: the pencil pass calls this for many modes and
+// ten unrolled rounds per call overflow the instruction cache.
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < 10; r++) {
         const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
         const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);

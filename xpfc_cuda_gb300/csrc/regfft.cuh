@@ -1,0 +1,106 @@
+// regfft.cuh -- two-level register FFT for lines of length N = P*Q.
+//
+// Q threads cooperate on a line; thread t holds element t + Q*j in v[j],
+// j in [0, P), both on entry and on exit.  With n = Q a + b, k = c + P d:
+//   X[c + P d] = sum_b W_Q^{bd} W_N^{bc} sum_a x[Q a + b] W_P^{ac}
+// so thread t (= b) does one P-point DFT over its own registers, multiplies by
+// W_N^{tc}, one shared-memory transpose hands column c to thread c mod Q, and
+// Q-point DFTs finish the line.  Global loads and stores move directly
+// between registers and memory in the t + Q j pattern, which is coalesced
+// across the threads of neighbouring lines (columns) or within a row.
+#pragma once
+#include "fft_core.cuh"
+
+namespace xpfc {
+
+template <int N> struct RP { static constexpr bool ok = false; static constexpr int P = 1, Q = 1; };
+template <> struct RP<64> { static constexpr bool ok = true; static constexpr int P = 8, Q = 8; };
+template <> struct RP<128> { static constexpr bool ok = true; static constexpr int P = 16, Q = 8; };
+template <> struct RP<256> { static constexpr bool ok = true; static constexpr int P = 16, Q = 16; };
+
+// Transpose scratch of one line: P rows of QP slots (QP odd: conflict-free
+// column reads), lines LPITCH apart.
+template <int N> struct RPad {
+    static constexpr int P = RP<N>::P, Q = RP<N>::Q;
+    static constexpr int QP = Q + 1;
+    // line pitch (complex elements) for lines that sit side by side in a warp:
+    // FP32 column kernels want pitch = 2 mod 16, FP32 row kernels 8 mod 16,
+    // FP64 an odd pitch.
+    template <int MOD, int REM> static constexpr int pitch() {
+        int p = P * QP;
+        while (p % MOD != REM) p++;
+        return p;
+    }
+};
+
+// v: P registers (element t + Q j).  buf: this line's scratch.  tw: W_N^k.
+// Every thread of the block must call it (two __syncthreads inside).
+template <typename T, int N, int DIR>
+__device__ __forceinline__ void reg_fft(cplx<T> *v, int t, cplx<T> *buf, const cplx<T> *__restrict__ tw) {
+    constexpr int P = RP<N>::P, Q = RP<N>::Q, M = P / Q, QP = RPad<N>::QP;
+    static_assert(P % Q == 0, "P must be a multiple of Q");
+    dftR<P, DIR, T>(v);
+#pragma unroll
+    for (int c = 1; c < P; c++) v[c] = twmul<DIR>(v[c], tw[t * c]);
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < P; c++) buf[c * QP + t] = v[c];
+    __syncthreads();
+    cplx<T> u[P];
+#pragma unroll
+    for (int m = 0; m < M; m++)
+#pragma unroll
+        for (int b = 0; b < Q; b++) u[m * Q + b] = buf[(t + Q * m) * QP + b];
+#pragma unroll
+    for (int m = 0; m < M; m++) dftR<Q, DIR, T>(u + m * Q);
+#pragma unroll
+    for (int m = 0; m < M; m++)
+#pragma unroll
+        for (int d = 0; d < Q; d++) v[m + M * d] = u[m * Q + d];
+}
+
+// Two lines (e.g. the state and the nonlinear term of one pencil) through
+// the same pattern, sharing the two barriers.
+template <typename T, int N, int DIR>
+__device__ __forceinline__ void reg_fft2(cplx<T> *v, cplx<T> *w, int t, cplx<T> *bufv, cplx<T> *bufw,
+                                         const cplx<T> *__restrict__ tw) {
+    constexpr int P = RP<N>::P, Q = RP<N>::Q, M = P / Q, QP = RPad<N>::QP;
+    dftR<P, DIR, T>(v);
+    dftR<P, DIR, T>(w);
+#pragma unroll
+    for (int c = 1; c < P; c++) {
+        const cplx<T> tc = tw[t * c];
+        v[c] = twmul<DIR>(v[c], tc);
+        w[c] = twmul<DIR>(w[c], tc);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < P; c++) {
+        bufv[c * QP + t] = v[c];
+        bufw[c * QP + t] = w[c];
+    }
+    __syncthreads();
+    cplx<T> u[P];
+#pragma unroll
+    for (int m = 0; m < M; m++)
+#pragma unroll
+        for (int b = 0; b < Q; b++) u[m * Q + b] = bufv[(t + Q * m) * QP + b];
+#pragma unroll
+    for (int m = 0; m < M; m++) dftR<Q, DIR, T>(u + m * Q);
+#pragma unroll
+    for (int m = 0; m < M; m++)
+#pragma unroll
+        for (int d = 0; d < Q; d++) v[m + M * d] = u[m * Q + d];
+#pragma unroll
+    for (int m = 0; m < M; m++)
+#pragma unroll
+        for (int b = 0; b < Q; b++) u[m * Q + b] = bufw[(t + Q * m) * QP + b];
+#pragma unroll
+    for (int m = 0; m < M; m++) dftR<Q, DIR, T>(u + m * Q);
+#pragma unroll
+    for (int m = 0; m < M; m++)
+#pragma unroll
+        for (int d = 0; d < Q; d++) w[m + M * d] = u[m * Q + d];
+}
+
+}  // namespace xpfc

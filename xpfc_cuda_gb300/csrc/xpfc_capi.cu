@@ -252,6 +252,18 @@ static KSpace make_kspace(const xpfc_ctx *ctx, bool dbl) {
     ks.noise_on = p.noise_amp != 0.0;
     ks.noise_scale = p.noise_amp * std::sqrt((double)ctx->ncells);
     ks.noise_seed = p.noise_seed;
+    ks.f_dk0sq = (float)ks.dk0sq;
+    ks.f_dk1sq = (float)ks.dk1sq;
+    ks.f_dk2sq = (float)ks.dk2sq;
+    ks.f_dt = (float)ks.dt;
+    ks.f_Mo = (float)ks.Mo;
+    ks.f_eps = (float)ks.eps;
+    ks.f_noise_scale = (float)ks.noise_scale;
+    for (int i = 0; i < 8; i++) {
+        ks.f_pk_k[i] = (float)ks.pk_k[i];
+        ks.f_pk_inv2a2[i] = (float)ks.pk_inv2a2[i];
+        ks.f_pk_dw[i] = (float)ks.pk_dw[i];
+    }
     return ks;
 }
 
@@ -413,6 +425,8 @@ static double *staged_buf(xpfc_ctx *ctx, int b) {
 // ---------------------------------------------------------------------------
 // transforms on one field buffer of type T (packed spectrum <-> real)
 // ---------------------------------------------------------------------------
+// Forward transform of everything but the pencil axis: the rows (unless
+// do_rows is false) and, in 3-D, the y columns.
 template <typename T>
 static int fft_forward_xy(xpfc_ctx *ctx, void *buf, bool do_rows) {
     const bool dbl = sizeof(T) == 8;
@@ -426,6 +440,7 @@ static int fft_forward_xy(xpfc_ctx *ctx, void *buf, bool do_rows) {
         ra.scale = 1.0;
         XPFC_LAUNCH(ctx, launch_row<T>(ROW_FWD, ctx->L0, ra, tw0, tw2, ctx->stream, nullptr));
     }
+    if (!ctx->three_d) return XPFC_OK;
     ColArgs ca{};
     ca.in = buf;
     ca.out = buf;

@@ -275,6 +275,9 @@ struct KSpace {
     double noise_scale;             // amp * sqrt(cells)
     unsigned long long noise_seed;
     long long step;
+    // the same constants in FP32 for the mixed path (no FP64 work per mode)
+    float f_dk0sq, f_dk1sq, f_dk2sq, f_dt, f_Mo, f_eps, f_noise_scale;
+    float f_pk_k[8], f_pk_inv2a2[8], f_pk_dw[8];
 };
 
 template <typename T> struct Coef { T A, B, c2, k2; };
@@ -291,21 +294,68 @@ __device__ __forceinline__ Coef<T> kcoef(const KSpace &ks, int i0, int i1, int i
         r.A = e[0]; r.B = e[1]; r.c2 = e[2]; r.k2 = e[3];
         return r;
     }
-    const T k2 = (T)ks.dk0sq * (T)(i0 * i0) + (T)ks.dk1sq * (T)(s1 * s1) + (T)ks.dk2sq * (T)(s2 * s2);
+    const bool f = sizeof(T) == 4;
+    const T k2 = (f ? (T)ks.f_dk0sq : (T)ks.dk0sq) * (T)(i0 * i0) + (f ? (T)ks.f_dk1sq : (T)ks.dk1sq) * (T)(s1 * s1) +
+                 (f ? (T)ks.f_dk2sq : (T)ks.dk2sq) * (T)(s2 * s2);
     const T kk = sqrt(k2);
     T c2 = (T)0;
     for (int p = 0; p < ks.npeaks; p++) {
-        const T d = kk - (T)ks.pk_k[p];
-        const T v = (T)ks.pk_dw[p] * exp(-(d * d) * (T)ks.pk_inv2a2[p]);
+        const T d = kk - (f ? (T)ks.f_pk_k[p] : (T)ks.pk_k[p]);
+        const T v = (f ? (T)ks.f_pk_dw[p] : (T)ks.pk_dw[p]) * exp(-(d * d) * (f ? (T)ks.f_pk_inv2a2[p] : (T)ks.pk_inv2a2[p]));
         c2 = ks.envelope == 0 ? c2 + v : (p == 0 || v > c2 ? v : c2);
     }
-    const T dt = (T)ks.dt, Mo = (T)ks.Mo;
-    const T den = ((T)1 + k2 * dt * Mo * ((T)1 - (T)ks.eps) - k2 * Mo * dt * c2);
+    const T dt = f ? (T)ks.f_dt : (T)ks.dt, Mo = f ? (T)ks.f_Mo : (T)ks.Mo, eps = f ? (T)ks.f_eps : (T)ks.eps;
+    const T den = ((T)1 + k2 * dt * Mo * ((T)1 - eps) - k2 * Mo * dt * c2);
     r.A = (T)1 / den;
     r.B = -(k2 * Mo * dt) / den;
     r.c2 = c2;
     r.k2 = k2;
     return r;
+}
+
+// Box-Muller of two 32-bit draws: u1 = (a+1) 2^-32 in (0,1], u2 = b 2^-32.
+// FP32 uses the hardware log/sin/cos approximations (the noise only needs
+// its distribution); FP64 the accurate functions.
+template <typename T>
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T &g0, T &g1) {
+    if (sizeof(T) == 8) {
+        const double u1 = ((double)a + 1.0) * 2.3283064365386963e-10;
+        const double u2 = (double)b * 2.3283064365386963e-10;
+        const double rr = sqrt(-2.0 * log(u1));
+        double sn, cs;
+        sincospi(2.0 * u2, &sn, &cs);
+        g0 = (T)(rr * cs);
+        g1 = (T)(rr * sn);
+    } else {
+        const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
+        const float u2 = (float)b * 2.3283064365386963e-10f;
+        const float rr = sqrtf(-2.0f * __logf(u1));
+        float sn, cs;
+        __sincosf(6.28318530717958647692f * u2, &sn, &cs);
+        g0 = (T)(rr * cs);
+        g1 = (T)(rr * sn);
+    }
+}
+
+// Philox draw for a canonical mode (c0, c1, c2): the slowest axis (z in 3-D,
+// y in 2-D) is folded in half; the lower half takes outputs 0,1, the upper 2,3.
+__device__ __forceinline__ uint4 noise_draw(const KSpace &ks, int c0, int c1, int c2, bool &upper) {
+    long long ctr;
+    if (ks.n2 > 1) {
+        upper = 2 * c2 >= ks.n2;
+        ctr = ((long long)(c2 % (ks.n2 / 2)) * ks.n1 + c1) * ks.n0 + c0;
+    } else {
+        upper = 2 * c1 >= ks.n1;
+        ctr = (long long)(c1 % (ks.n1 / 2)) * ks.n0 + c0;
+    }
+    const unsigned long long stream = 1ull + (unsigned long long)ks.step;
+    return philox4x32_10(make_uint4((uint32_t)ctr, (uint32_t)((unsigned long long)ctr >> 32), (uint32_t)stream,
+                                    (uint32_t)(stream >> 32)),
+                         make_uint2((uint32_t)ks.noise_seed, (uint32_t)(ks.noise_seed >> 32)));
+}
+
+template <typename T> __device__ __forceinline__ T noise_amp_of(const KSpace &ks, T k2) {
+    return (sizeof(T) == 4 ? (T)ks.f_noise_scale : (T)ks.noise_scale) * sqrt(k2);
 }
 
 // conserved noise xi_k = amp sqrt(cells) |k| g_k at full-grid mode (i0,i1,i2),
@@ -316,40 +366,31 @@ __device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, int i0, int i1, in
     const bool edge = (i0 == 0) || (2 * i0 == ks.n0);
     const bool selfc = edge && j1 == i1 && j2 == i2;
     bool canon = true;
-    long long ci;
-    if (edge) {
-        const long long l = (long long)i2 * ks.n1 + i1, lm = (long long)j2 * ks.n1 + j1;
-        canon = l <= lm;
-        ci = canon ? l * ks.n0 + i0 : lm * ks.n0 + i0;
-    } else {
-        ci = ((long long)i2 * ks.n1 + i1) * ks.n0 + i0;
-    }
-    const unsigned long long stream = 1ull + (unsigned long long)ks.step;
-    uint4 o = philox4x32_10(make_uint4((uint32_t)ci, (uint32_t)((unsigned long long)ci >> 32), (uint32_t)stream,
-                                       (uint32_t)(stream >> 32)),
-                            make_uint2((uint32_t)ks.noise_seed, (uint32_t)(ks.noise_seed >> 32)));
+    if (edge) canon = (long long)i2 * ks.n1 + i1 <= (long long)j2 * ks.n1 + j1;
+    bool upper;
+    const uint4 o = canon ? noise_draw(ks, i0, i1, i2, upper) : noise_draw(ks, i0, j1, j2, upper);
     T g0, g1;
-    if (sizeof(T) == 8) {
-        const double u1 = ((double)o.x + 1.0) * 2.3283064365386963e-10;
-        const double u2 = (double)o.y * 2.3283064365386963e-10;
-        const double rr = sqrt(-2.0 * log(u1));
-        double sn, cs;
-        sincospi(2.0 * u2, &sn, &cs);
-        g0 = (T)(rr * cs);
-        g1 = (T)(rr * sn);
-    } else {
-        const float u1 = ((float)o.x + 1.0f) * 2.3283064365386963e-10f;
-        const float u2 = (float)o.y * 2.3283064365386963e-10f;
-        const float rr = sqrtf(-2.0f * logf(u1));
-        float sn, cs;
-        sincospif(2.0f * u2, &sn, &cs);
-        g0 = (T)(rr * cs);
-        g1 = (T)(rr * sn);
-    }
-    const T amp = (T)ks.noise_scale * sqrt(k2);
+    box_muller<T>(upper ? o.z : o.x, upper ? o.w : o.y, g0, g1);
+    const T amp = noise_amp_of<T>(ks, k2);
     if (selfc) return mk<T>(amp * g0, (T)0);
     const T h = (T)0.70710678118654752440;
     return mk<T>(amp * g0 * h, (canon ? amp : -amp) * g1 * h);
+}
+
+// Noise of two interior modes (0 < i0 < n0/2) whose slow coordinates are s
+// and s + n_slow/2: one Philox call, both halves of its output.
+template <typename T>
+__device__ __forceinline__ void noise_pair_interior(const KSpace &ks, int i0, int i1, int i2, T k2a, T k2b,
+                                                    cplx<T> &na, cplx<T> &nb) {
+    bool upper;
+    const uint4 o = noise_draw(ks, i0, i1, i2, upper);
+    T g0, g1, g2, g3;
+    box_muller<T>(o.x, o.y, g0, g1);
+    box_muller<T>(o.z, o.w, g2, g3);
+    const T h = (T)0.70710678118654752440;
+    const T a = noise_amp_of<T>(ks, k2a) * h, b = noise_amp_of<T>(ks, k2b) * h;
+    na = mk<T>(a * g0, a * g1);
+    nb = mk<T>(b * g2, b * g3);
 }
 
 // ---------------------------------------------------------------------------

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "xpfc_kernels.cuh"
+#include "xpfc_regkernels.cuh"
 
 namespace xpfc {
 

@@ -1,0 +1,338 @@
+// xpfc_regkernels.cuh -- the step's passes built on the two-level register
+// FFT (regfft.cuh) for line lengths with a register plan (64, 128, 256).
+// Same arguments, layouts and results as the shared-memory Stockham passes
+// of xpfc_kernels.cuh, which serve every other length.
+#pragma once
+#include "regfft.cuh"
+#include "xpfc_kernels.cuh"
+
+namespace xpfc {
+
+constexpr unsigned FULLMASK = 0xffffffffu;
+
+template <typename T>
+__device__ __forceinline__ cplx<T> shfl_c(cplx<T> v, int src) {
+    return mk<T>(__shfl_sync(FULLMASK, v.x, src), __shfl_sync(FULLMASK, v.y, src));
+}
+
+// ---------------------------------------------------------------------------
+// column pass (C2C along a strided axis), TX columns per block
+// ---------------------------------------------------------------------------
+template <typename T, int N> struct RColShape {
+    static constexpr int Q = RP<N>::Q, P = RP<N>::P;
+    static constexpr int TX = sizeof(T) == 4 ? 16 : 8;
+    static constexpr int THREADS = TX * Q;
+    static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
+    static constexpr size_t SMEM = sizeof(cplx<T>) * (N + (size_t)TX * LP);
+};
+
+template <typename T, int N, int DIR>
+__global__ void __launch_bounds__(RColShape<T, N>::THREADS)
+col_kernel_reg(ColArgs args, const cplx<T> *__restrict__ twN) {
+    using S = RColShape<T, N>;
+    constexpr int TX = S::TX, Q = S::Q, P = S::P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *buf = stw + N;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < N; i += S::THREADS) stw[i] = twN[i];
+    const int c = tid % TX, t = tid / TX;
+    const bool cvalid = (int)blockIdx.x * TX + c < args.ncols;
+    const long long base = (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride + c;
+    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + base;
+    cplx<T> v[P];
+#pragma unroll
+    for (int j = 0; j < P; j++) v[j] = cvalid ? gin[(long long)(t + Q * j) * args.es] : mk<T>((T)0, (T)0);
+    __syncthreads();
+    reg_fft<T, N, DIR>(v, t, buf + c * S::LP, stw);
+    if (!cvalid) return;
+    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + base;
+    const T sc = (T)args.scale;
+#pragma unroll
+    for (int j = 0; j < P; j++)
+        gout[(long long)(t + Q * j) * args.es] = (args.scale != 1.0) ? cscale(v[j], sc) : v[j];
+}
+
+// ---------------------------------------------------------------------------
+// row pass: C2R unpack, inverse FFT, real-space op, forward FFT, R2C pack.
+// Q threads per row; the pairing of k with L - k uses warp shuffles.
+// ---------------------------------------------------------------------------
+template <typename T, int N> struct RRowShape {
+    static constexpr int Q = RP<N>::Q, P = RP<N>::P;
+    static constexpr int ROWS = 256 / Q;
+    static constexpr int THREADS = ROWS * Q;
+    static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 8>() : RPad<N>::template pitch<2, 1>();
+    static constexpr size_t SMEM = sizeof(cplx<T>) * (2 * N + (size_t)ROWS * LP) + sizeof(double) * 32 * NQ_ROW;
+};
+
+// Z[k] = (Xk + conj Xc) + i (Xk - conj Xc) W_{2N}^{-k} for this thread's k = t + Q j
+template <typename T, int N>
+__device__ __forceinline__ void reg_unpack(cplx<T> *v, int t, int lane, const cplx<T> *__restrict__ tw2) {
+    constexpr int Q = RP<N>::Q, P = RP<N>::P;
+    const int partner = (t == 0) ? lane : lane + Q - 2 * t;
+    cplx<T> z[P];
+#pragma unroll
+    for (int j = 0; j < P; j++) {
+        const cplx<T> sh = shfl_c<T>(v[P - 1 - j], partner);
+        const int k = t + Q * j;
+        if (k == 0) {
+            const cplx<T> p = v[0];
+            z[0] = mk<T>(p.x + p.y, p.x - p.y);
+            continue;
+        }
+        const cplx<T> xc = (t == 0) ? v[P - j] : sh;   // X[N - k]
+        const cplx<T> xk = v[j];
+        const cplx<T> e = cadd(xk, cconj(xc));
+        const cplx<T> o = cmulc(csub(xk, cconj(xc)), tw2[k]);
+        z[j] = cadd(e, cmuli<1>(o));
+    }
+#pragma unroll
+    for (int j = 0; j < P; j++) v[j] = z[j];
+}
+
+// X[k] = ((Zk + conj Zc) - i W_{2N}^k (Zk - conj Zc))/2, slot 0 = (X0, XN)
+template <typename T, int N>
+__device__ __forceinline__ void reg_pack(cplx<T> *v, int t, int lane, const cplx<T> *__restrict__ tw2) {
+    constexpr int Q = RP<N>::Q, P = RP<N>::P;
+    const int partner = (t == 0) ? lane : lane + Q - 2 * t;
+    const T h = (T)0.5;
+    cplx<T> z[P];
+#pragma unroll
+    for (int j = 0; j < P; j++) {
+        const cplx<T> sh = shfl_c<T>(v[P - 1 - j], partner);
+        const int k = t + Q * j;
+        if (k == 0) {
+            const cplx<T> p = v[0];
+            z[0] = mk<T>(p.x + p.y, p.x - p.y);
+            continue;
+        }
+        const cplx<T> zc = (t == 0) ? v[P - j] : sh;   // Z[N - k]
+        const cplx<T> zk = v[j];
+        const cplx<T> e = cadd(zk, cconj(zc));
+        const cplx<T> o = cmul(csub(zk, cconj(zc)), tw2[k]);
+        z[j] = cscale(csub(e, cmuli<1>(o)), h);
+    }
+#pragma unroll
+    for (int j = 0; j < P; j++) v[j] = z[j];
+}
+
+template <typename T, int N, int MODE>
+__global__ void __launch_bounds__(RRowShape<T, N>::THREADS)
+row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__restrict__ tw2N) {
+    using S = RRowShape<T, N>;
+    constexpr int Q = S::Q, P = S::P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *stw2 = stw + N;
+    cplx<T> *buf = stw2 + N;
+    double *sred = reinterpret_cast<double *>(buf + S::ROWS * S::LP);
+    const int tid = threadIdx.x;
+    for (int i = tid; i < N; i += S::THREADS) {
+        stw[i] = twN[i];
+        stw2[i] = tw2N[i];
+    }
+    const int r = tid / Q, t = tid % Q, lane = tid & 31;
+    const long long row = (long long)blockIdx.x * S::ROWS + r;
+    const bool valid = row < args.nrows;
+    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + row * N + t;
+    cplx<T> v[P];
+#pragma unroll
+    for (int j = 0; j < P; j++) v[j] = valid ? gin[Q * j] : mk<T>((T)0, (T)0);
+    __syncthreads();
+    cplx<T> *line = buf + r * S::LP;
+
+    if (MODE == ROW_INV || MODE == ROW_FUSED) {
+        reg_unpack<T, N>(v, t, lane, stw2);
+        reg_fft<T, N, +1>(v, t, line, stw);
+    }
+    if (MODE == ROW_INV) {
+        const T sc = (T)args.scale;
+#pragma unroll
+        for (int j = 0; j < P; j++) v[j] = cscale(v[j], sc);
+    } else if (MODE == ROW_FUSED || MODE == ROW_NL_FWD) {
+        double acc[NQ_ROW] = {0.0, 0.0, 0.0, 0.0};
+        const T sc = (T)args.scale;
+        const T a = (T)args.a, b = (T)args.b;
+        T *rout = args.real_out ? reinterpret_cast<T *>(args.real_out) + row * (2 * N) : nullptr;
+#pragma unroll
+        for (int j = 0; j < P; j++) {
+            T x0 = v[j].x, x1 = v[j].y;
+            if (MODE == ROW_FUSED) { x0 *= sc; x1 *= sc; }
+            const int m = t + Q * j;
+            if (rout && valid) { rout[2 * m] = x0; rout[2 * m + 1] = x1; }
+            const T p20 = powi(x0, 2, args.ref_compat), p21 = powi(x1, 2, args.ref_compat);
+            const T p30 = powi(x0, 3, args.ref_compat), p31 = powi(x1, 3, args.ref_compat);
+            if (args.want_red && valid) {
+                acc[0] += (double)x0 + (double)x1;
+                acc[1] += (double)p20 + (double)p21;
+                acc[2] += (double)p30 + (double)p31;
+                acc[3] += (double)powi(x0, 4, args.ref_compat) + (double)powi(x1, 4, args.ref_compat);
+            }
+            v[j] = mk<T>(-a * p20 + b * p30, -a * p21 + b * p31);
+        }
+        if (args.want_red) block_reduce_store<NQ_ROW>(acc, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
+    }
+    if (MODE != ROW_INV) {
+        reg_fft<T, N, -1>(v, t, line, stw);
+        reg_pack<T, N>(v, t, lane, stw2);
+    }
+    if (!valid) return;
+    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + row * N + t;
+#pragma unroll
+    for (int j = 0; j < P; j++) gout[Q * j] = v[j];
+}
+
+// ---------------------------------------------------------------------------
+// pencil pass (last axis): forward FFT of S and W, semi-implicit update in
+// registers, k-space sums, inverse FFT of S.  3-D blocks pair rows p and
+// n1 - p (NG = 2) so that slot 0 finds its mirror mode in the block.
+// ---------------------------------------------------------------------------
+template <typename T, int N, int NG> struct RPenShape {
+    static constexpr int Q = RP<N>::Q, P = RP<N>::P;
+    static constexpr int TX = sizeof(T) == 4 ? 8 : 4;
+    static constexpr int THREADS = TX * Q * NG;
+    static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
+    static constexpr int LINES = TX * NG;
+    static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
+};
+
+// The update of one mode given its coefficients and noise (zero when off).
+template <typename T>
+__device__ __forceinline__ cplx<T> update_coef(const KSpace &ks, const PenArgs &args, const Coef<T> &cf, int i0,
+                                               int i1, int i2, cplx<T> xs, cplx<T> xw, cplx<T> noise, double *acc,
+                                               double weight) {
+    const cplx<T> num = cadd(xs, noise);
+    cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
+    if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)args.pin_value, (T)0);
+    if (args.want_red) {
+        const double xr = xs.x, xi = xs.y, k2 = cf.k2, c2 = cf.c2;
+        acc[0] += weight * c2 * (xr * xr + xi * xi);
+        const double rr = ((double)xn.x - xr) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xr + (double)xw.x);
+        const double ri = ((double)xn.y - xi) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xi + (double)xw.y);
+        acc[1] += weight * (rr * rr + ri * ri);
+    }
+    return xn;
+}
+
+template <typename T>
+__device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const PenArgs &args, int i0, int i1, int i2,
+                                               cplx<T> xs, cplx<T> xw, double *acc, double weight) {
+    const Coef<T> cf = kcoef<T>(ks, i0, i1, i2);
+    cplx<T> num = xs;
+    if (ks.noise_on) num = cadd(num, noise_at<T>(ks, i0, i1, i2, cf.k2));
+    cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
+    if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)args.pin_value, (T)0);
+    if (args.want_red) {
+        const double xr = xs.x, xi = xs.y, k2 = cf.k2, c2 = cf.c2;
+        acc[0] += weight * c2 * (xr * xr + xi * xi);
+        const double rr = ((double)xn.x - xr) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xr + (double)xw.x);
+        const double ri = ((double)xn.y - xi) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xi + (double)xw.y);
+        acc[1] += weight * (rr * rr + ri * ri);
+    }
+    return xn;
+}
+
+template <typename T, int N, int NG>
+__global__ void __launch_bounds__(RPenShape<T, N, NG>::THREADS)
+pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
+    using S = RPenShape<T, N, NG>;
+    constexpr int TX = S::TX, Q = S::Q, P = S::P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *bufS = stw + N;
+    cplx<T> *bufW = bufS + S::LINES * S::LP;
+    double *sred = reinterpret_cast<double *>(bufW + S::LINES * S::LP);
+    const int tid = threadIdx.x;
+    for (int i = tid; i < N; i += S::THREADS) stw[i] = twN[i];
+
+    const int c = tid % TX, t = (tid / TX) % Q, g = tid / (TX * Q);
+    const int p = blockIdx.y;
+    const int y1 = p, y2 = (NG == 2) ? (ks.n1 - p) % ks.n1 : p;
+    const int G = (NG == 2 && y2 != y1) ? 2 : 1;
+    const int yg = (g == 0) ? y1 : y2;
+    const int kx0 = blockIdx.x * TX;
+    const bool valid = (g < G) && (kx0 + c < args.L0);
+    const long long off = (long long)yg * args.gstride + kx0 + c;
+    cplx<T> *gS = reinterpret_cast<cplx<T> *>(args.S) + off;
+    const cplx<T> *gW = reinterpret_cast<const cplx<T> *>(args.W) + off;
+    cplx<T> vs[P], vw[P];
+#pragma unroll
+    for (int j = 0; j < P; j++) {
+        const long long e = (long long)(t + Q * j) * args.es;
+        vs[j] = valid ? gS[e] : mk<T>((T)0, (T)0);
+        vw[j] = valid ? gW[e] : mk<T>((T)0, (T)0);
+    }
+    __syncthreads();
+    const int ln = g * TX + c;
+    reg_fft2<T, N, -1>(vs, vw, t, bufS + ln * S::LP, bufW + ln * S::LP, stw);
+
+    double acc[NQ_PEN] = {0.0, 0.0};
+    const T sc = (T)args.scale;
+    const int nh = args.L0;
+    const cplx<T> zero = mk<T>((T)0, (T)0);
+
+    // slot 0 (only in the block holding kx' = 0): the kx = 0 and kx = n0/2
+    // planes separate with the mirror mode (-k1, -k2).  Those pencils go
+    // through shared memory and every thread of the block takes a share,
+    // which keeps this rare path small in the instruction stream.
+    if (kx0 == 0) {
+        cplx<T> *outS = bufW + 2 * N;                  // after the [group][kz] publish areas
+        __syncthreads();
+        if (c == 0 && g < G) {
+#pragma unroll
+            for (int j = 0; j < P; j++) {
+                bufS[g * N + t + Q * j] = vs[j];
+                bufW[g * N + t + Q * j] = vw[j];
+            }
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int idx = tid; idx < G * N; idx += S::THREADS) {
+            const int gg = idx / N, kz = idx % N;
+            const int yy = (gg == 0) ? y1 : y2;
+            const int i1 = args.three_d ? yy : kz;
+            const int i2 = args.three_d ? kz : 0;
+            const int gm = (G == 2) ? 1 - gg : gg;
+            const int kzm = (N - kz) % N;
+            const cplx<T> xs = bufS[gg * N + kz], xw = bufW[gg * N + kz];
+            const cplx<T> ps = bufS[gm * N + kzm], pw = bufW[gm * N + kzm];
+            const T h = (T)0.5;
+            const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
+            const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
+            const cplx<T> x0 = update_mode<T>(ks, args, 0, i1, i2, s0, w0, acc, 1.0);
+            const cplx<T> xN = update_mode<T>(ks, args, nh, i1, i2, sN, wN, acc, 1.0);
+            outS[gg * N + kz] = cscale(cadd(x0, cmuli<1>(xN)), sc);
+        }
+        __syncthreads();
+        if (c == 0 && g < G) {
+#pragma unroll
+            for (int j = 0; j < P; j++) vs[j] = outS[g * N + t + Q * j];
+        }
+    }
+    if (valid && kx0 + c != 0) {
+        // interior columns: modes j and j + P/2 sit at kz and kz + N/2 and
+        // share one Philox draw
+        const int i0 = kx0 + c;
+#pragma unroll
+        for (int j = 0; j < P / 2; j++) {
+            const int kza = t + Q * j, kzb = kza + N / 2;
+            const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
+            const int i1b = args.three_d ? yg : kzb, i2b = args.three_d ? kzb : 0;
+            const Coef<T> ca = kcoef<T>(ks, i0, i1a, i2a), cb = kcoef<T>(ks, i0, i1b, i2b);
+            cplx<T> na = zero, nb = zero;
+            if (ks.noise_on) noise_pair_interior<T>(ks, i0, i1a, i2a, ca.k2, cb.k2, na, nb);
+            vs[j] = cscale(update_coef<T>(ks, args, ca, i0, i1a, i2a, vs[j], vw[j], na, acc, 2.0), sc);
+            vs[j + P / 2] = cscale(update_coef<T>(ks, args, cb, i0, i1b, i2b, vs[j + P / 2], vw[j + P / 2], nb, acc,
+                                                  2.0), sc);
+        }
+    }
+    if (args.want_red)
+        block_reduce_store<NQ_PEN>(acc, args.partials + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * NQ_PEN, sred);
+    if (!args.update) return;
+    reg_fft<T, N, +1>(vs, t, bufS + ln * S::LP, stw);
+    if (!valid) return;
+#pragma unroll
+    for (int j = 0; j < P; j++) gS[(long long)(t + Q * j) * args.es] = vs[j];
+}
+
+}  // namespace xpfc
