@@ -24,9 +24,30 @@ template <> struct ctype<double> { using type = double2; };
 template <typename T> using cplx = typename ctype<T>::type;
 
 template <typename T> __device__ __forceinline__ cplx<T> mk(T x, T y) { cplx<T> r; r.x = x; r.y = y; return r; }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+// FP32 complex values travel as one 64-bit register pair, so additions,
+// subtractions and real scalings use Blackwell's packed f32x2 arithmetic
+// (one instruction per complex operation instead of two).
+__device__ __forceinline__ unsigned long long f2pack(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 f2unpack(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2pack(a)), "l"(f2pack(b)));
+    return f2unpack(d);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2pack(a)), "l"(f2pack(b)));
+    return f2unpack(d);
+}
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -43,7 +64,11 @@ __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
 }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2pack(a)), "l"(f2pack(make_float2(s, s))));
+    return f2unpack(d);
+}
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 // multiply by +i (s = +1) or -i (s = -1)
 template <int S> __device__ __forceinline__ float2 cmuli(float2 a) {
@@ -90,13 +115,32 @@ template <int DIR, typename C, typename T> __device__ __forceinline__ C rot16(C 
     return DIR < 0 ? mk<T>(a.x * c + a.y * s, a.y * c - a.x * s) : mk<T>(a.x * c - a.y * s, a.y * c + a.x * s);
 }
 
+// a * W16^E with the exact special cases spelled out (IEEE arithmetic may
+// not drop a multiplication by 0, so W16^0, ^4, ^8 and the sqrt(1/2) pairs
+// ^2, ^6 get their own short forms); E in [0, 9]
+template <int E, int DIR, typename T> __device__ __forceinline__ cplx<T> tw16c(cplx<T> a) {
+    const T r = (T)0.70710678118654752440;
+    if constexpr (E == 0) return a;
+    else if constexpr (E == 4) return cmuli<DIR>(a);                     // forward: -i
+    else if constexpr (E == 8) return mk<T>(-a.x, -a.y);
+    else if constexpr (E == 2)                                           // forward: (1 - i)/sqrt 2
+        return DIR < 0 ? mk<T>((a.x + a.y) * r, (a.y - a.x) * r) : mk<T>((a.x - a.y) * r, (a.y + a.x) * r);
+    else if constexpr (E == 6)                                           // forward: -(1 + i)/sqrt 2
+        return DIR < 0 ? mk<T>((a.y - a.x) * r, -(a.x + a.y) * r) : mk<T>(-(a.x + a.y) * r, (a.x - a.y) * r);
+    else if constexpr (E == 9) {
+        const cplx<T> q = rot16<DIR, cplx<T>, T>(a, 1);
+        return mk<T>(-q.x, -q.y);
+    } else
+        return rot16<DIR, cplx<T>, T>(a, E);
+}
+
 template <int DIR, typename T> __device__ __forceinline__ void dft8(cplx<T> *v) {
     // 8 = 2 x 4 (decimation in time): E = DFT4(even), O = DFT4(odd), X_k = E_k + W8^k O_k
     dft4<DIR>(v[0], v[2], v[4], v[6]);
     dft4<DIR>(v[1], v[3], v[5], v[7]);
-    cplx<T> o1 = rot16<DIR, cplx<T>, T>(v[3], 2);
+    cplx<T> o1 = tw16c<2, DIR, T>(v[3]);
     cplx<T> o2 = cmuli<DIR>(v[5]);
-    cplx<T> o3 = rot16<DIR, cplx<T>, T>(v[7], 6);
+    cplx<T> o3 = tw16c<6, DIR, T>(v[7]);
     cplx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
     v[0] = cadd(e0, v[1]);
     v[4] = csub(e0, v[1]);
@@ -108,26 +152,23 @@ template <int DIR, typename T> __device__ __forceinline__ void dft8(cplx<T> *v) 
     v[7] = csub(e3, o3);
 }
 
-// a * W16^e for e in [0, 9] (W16^9 = -W16^1)
-template <int DIR, typename T> __device__ __forceinline__ cplx<T> tw16(cplx<T> a, int e) {
-    if (e <= 8) return rot16<DIR, cplx<T>, T>(a, e);
-    cplx<T> r = rot16<DIR, cplx<T>, T>(a, e - 8);
-    return mk<T>(-r.x, -r.y);
+template <int DIR, typename T, int N1> __device__ __forceinline__ void dft16_col(cplx<T> *v, cplx<T> *y) {
+    cplx<T> a = v[N1], b = v[N1 + 4], c = v[N1 + 8], d = v[N1 + 12];
+    dft4<DIR>(a, b, c, d);
+    y[N1 * 4 + 0] = a;
+    y[N1 * 4 + 1] = tw16c<N1, DIR, T>(b);
+    y[N1 * 4 + 2] = tw16c<2 * N1, DIR, T>(c);
+    y[N1 * 4 + 3] = tw16c<3 * N1, DIR, T>(d);
 }
 
 template <int DIR, typename T> __device__ __forceinline__ void dft16(cplx<T> *v) {
     // 16 = 4 x 4 with n = n1 + 4 n2, k = k2 + 4 k1:
     // Y[n1][k2] = DFT4_n2(x[n1 + 4 n2]) * W16^{n1 k2};  X[k2 + 4 k1] = DFT4_n1(Y[n1][k2])
     cplx<T> y[16];
-#pragma unroll
-    for (int n1 = 0; n1 < 4; n1++) {
-        cplx<T> a = v[n1], b = v[n1 + 4], c = v[n1 + 8], d = v[n1 + 12];
-        dft4<DIR>(a, b, c, d);
-        y[n1 * 4 + 0] = a;
-        y[n1 * 4 + 1] = tw16<DIR, T>(b, n1);
-        y[n1 * 4 + 2] = tw16<DIR, T>(c, 2 * n1);
-        y[n1 * 4 + 3] = tw16<DIR, T>(d, 3 * n1);
-    }
+    dft16_col<DIR, T, 0>(v, y);
+    dft16_col<DIR, T, 1>(v, y);
+    dft16_col<DIR, T, 2>(v, y);
+    dft16_col<DIR, T, 3>(v, y);
 #pragma unroll
     for (int k2 = 0; k2 < 4; k2++) {
         cplx<T> a = y[0 * 4 + k2], b = y[1 * 4 + k2], c = y[2 * 4 + k2], d = y[3 * 4 + k2];
@@ -294,10 +335,11 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NQ], double *__re
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and Box-Muller.
 // ---------------------------------------------------------------------------
-// The round loop stays rolled: the pencil pass calls this for many modes and
-// ten unrolled rounds per call overflow the instruction cache.
+// ROLLED keeps the round loop as a loop: code on rare paths stays small
+// (the instruction cache is the limit of the pencil pass).
+template <bool ROLLED = true>
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
-#pragma unroll 1
+#pragma unroll(ROLLED ? 1 : 10)
     for (int r = 0; r < 10; r++) {
         const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
         const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);

@@ -50,8 +50,13 @@ template <typename T, int L, int NG> struct PenShape {
 // ---------------------------------------------------------------------------
 // real-space op
 // ---------------------------------------------------------------------------
+// The reference's float power (power_functions.cu:47), kept out of line: it
+// runs only in reference-compatible mode and would otherwise be inlined at
+// every call site of the unrolled loops.
+static __device__ __noinline__ float ref_powf(float x, float p) { return powf(x, p); }
+
 template <typename T> __device__ __forceinline__ T powi(T x, int p, int ref_compat) {
-    if (ref_compat) return (T)powf((float)x, (float)p);   // power_functions.cu:47
+    if (ref_compat) return (T)ref_powf((float)x, (float)p);
     if (p == 2) return x * x;
     if (p == 3) return x * x * x;
     T s = x * x;
@@ -290,8 +295,14 @@ __device__ __forceinline__ Coef<T> kcoef(const KSpace &ks, int i0, int i1, int i
     Coef<T> r;
     if (ks.table) {
         const int m = i0 * i0 + s1 * s1 + s2 * s2;
-        const T *e = reinterpret_cast<const T *>(ks.table) + 4 * (size_t)m;
-        r.A = e[0]; r.B = e[1]; r.c2 = e[2]; r.k2 = e[3];
+        if constexpr (sizeof(T) == 4) {
+            const float4 e = __ldg(reinterpret_cast<const float4 *>(ks.table) + m);
+            r.A = e.x; r.B = e.y; r.c2 = e.z; r.k2 = e.w;
+        } else {
+            const double2 e0 = __ldg(reinterpret_cast<const double2 *>(ks.table) + 2 * (size_t)m);
+            const double2 e1 = __ldg(reinterpret_cast<const double2 *>(ks.table) + 2 * (size_t)m + 1);
+            r.A = e0.x; r.B = e0.y; r.c2 = e1.x; r.k2 = e1.y;
+        }
         return r;
     }
     const bool f = sizeof(T) == 4;
@@ -339,6 +350,7 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T &g0, T &g1)
 
 // Philox draw for a canonical mode (c0, c1, c2): the slowest axis (z in 3-D,
 // y in 2-D) is folded in half; the lower half takes outputs 0,1, the upper 2,3.
+template <bool ROLLED = true>
 __device__ __forceinline__ uint4 noise_draw(const KSpace &ks, int c0, int c1, int c2, bool &upper) {
     long long ctr;
     if (ks.n2 > 1) {
@@ -349,9 +361,9 @@ __device__ __forceinline__ uint4 noise_draw(const KSpace &ks, int c0, int c1, in
         ctr = (long long)(c1 % (ks.n1 / 2)) * ks.n0 + c0;
     }
     const unsigned long long stream = 1ull + (unsigned long long)ks.step;
-    return philox4x32_10(make_uint4((uint32_t)ctr, (uint32_t)((unsigned long long)ctr >> 32), (uint32_t)stream,
-                                    (uint32_t)(stream >> 32)),
-                         make_uint2((uint32_t)ks.noise_seed, (uint32_t)(ks.noise_seed >> 32)));
+    return philox4x32_10<ROLLED>(make_uint4((uint32_t)ctr, (uint32_t)((unsigned long long)ctr >> 32), (uint32_t)stream,
+                                            (uint32_t)(stream >> 32)),
+                                 make_uint2((uint32_t)ks.noise_seed, (uint32_t)(ks.noise_seed >> 32)));
 }
 
 template <typename T> __device__ __forceinline__ T noise_amp_of(const KSpace &ks, T k2) {
@@ -383,7 +395,7 @@ template <typename T>
 __device__ __forceinline__ void noise_pair_interior(const KSpace &ks, int i0, int i1, int i2, T k2a, T k2b,
                                                     cplx<T> &na, cplx<T> &nb) {
     bool upper;
-    const uint4 o = noise_draw(ks, i0, i1, i2, upper);
+    const uint4 o = noise_draw<false>(ks, i0, i1, i2, upper);
     T g0, g1, g2, g3;
     box_muller<T>(o.x, o.y, g0, g1);
     box_muller<T>(o.z, o.w, g2, g3);

@@ -116,7 +116,9 @@ __device__ __forceinline__ void reg_pack(cplx<T> *v, int t, int lane, const cplx
     for (int j = 0; j < P; j++) v[j] = z[j];
 }
 
-template <typename T, int N, int MODE>
+// RED: this launch also produces the real-space sums (diagnostics steps); a
+// separate instance keeps that code out of the hot loop of the other steps.
+template <typename T, int N, int MODE, bool RED>
 __global__ void __launch_bounds__(RRowShape<T, N>::THREADS)
 row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__restrict__ tw2N) {
     using S = RRowShape<T, N>;
@@ -162,7 +164,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
             if (rout && valid) { rout[2 * m] = x0; rout[2 * m + 1] = x1; }
             const T p20 = powi(x0, 2, args.ref_compat), p21 = powi(x1, 2, args.ref_compat);
             const T p30 = powi(x0, 3, args.ref_compat), p31 = powi(x1, 3, args.ref_compat);
-            if (args.want_red && valid) {
+            if (RED && valid) {
                 acc[0] += (double)x0 + (double)x1;
                 acc[1] += (double)p20 + (double)p21;
                 acc[2] += (double)p30 + (double)p31;
@@ -170,7 +172,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
             }
             v[j] = mk<T>(-a * p20 + b * p30, -a * p21 + b * p31);
         }
-        if (args.want_red) block_reduce_store<NQ_ROW>(acc, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
+        if (RED) block_reduce_store<NQ_ROW>(acc, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
     }
     if (MODE != ROW_INV) {
         reg_fft<T, N, -1>(v, t, line, stw);
@@ -194,17 +196,17 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
     static constexpr int LINES = TX * NG;
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
+    static constexpr int MINB = 1;
 };
 
 // The update of one mode given its coefficients and noise (zero when off).
-template <typename T>
-__device__ __forceinline__ cplx<T> update_coef(const KSpace &ks, const PenArgs &args, const Coef<T> &cf, int i0,
-                                               int i1, int i2, cplx<T> xs, cplx<T> xw, cplx<T> noise, double *acc,
-                                               double weight) {
+// (interior modes: never k = 0, so no pinning)
+template <typename T, bool RED>
+__device__ __forceinline__ cplx<T> update_coef(const KSpace &ks, const Coef<T> &cf, cplx<T> xs, cplx<T> xw,
+                                               cplx<T> noise, double *acc, double weight) {
     const cplx<T> num = cadd(xs, noise);
     cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
-    if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)args.pin_value, (T)0);
-    if (args.want_red) {
+    if (RED) {
         const double xr = xs.x, xi = xs.y, k2 = cf.k2, c2 = cf.c2;
         acc[0] += weight * c2 * (xr * xr + xi * xi);
         const double rr = ((double)xn.x - xr) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xr + (double)xw.x);
@@ -232,8 +234,8 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const PenArgs &
     return xn;
 }
 
-template <typename T, int N, int NG>
-__global__ void __launch_bounds__(RPenShape<T, N, NG>::THREADS)
+template <typename T, int N, int NG, bool RED>
+__global__ void __launch_bounds__(RPenShape<T, N, NG>::THREADS, RPenShape<T, N, NG>::MINB)
 pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     using S = RPenShape<T, N, NG>;
     constexpr int TX = S::TX, Q = S::Q, P = S::P;
@@ -321,12 +323,11 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const Coef<T> ca = kcoef<T>(ks, i0, i1a, i2a), cb = kcoef<T>(ks, i0, i1b, i2b);
             cplx<T> na = zero, nb = zero;
             if (ks.noise_on) noise_pair_interior<T>(ks, i0, i1a, i2a, ca.k2, cb.k2, na, nb);
-            vs[j] = cscale(update_coef<T>(ks, args, ca, i0, i1a, i2a, vs[j], vw[j], na, acc, 2.0), sc);
-            vs[j + P / 2] = cscale(update_coef<T>(ks, args, cb, i0, i1b, i2b, vs[j + P / 2], vw[j + P / 2], nb, acc,
-                                                  2.0), sc);
+            vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, 2.0), sc);
+            vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, 2.0), sc);
         }
     }
-    if (args.want_red)
+    if (RED)
         block_reduce_store<NQ_PEN>(acc, args.partials + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * NQ_PEN, sred);
     if (!args.update) return;
     reg_fft<T, N, +1>(vs, t, bufS + ln * S::LP, stw);
