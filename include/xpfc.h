@@ -198,6 +198,27 @@ int xpfc_write_vtk(const char *path, const double *host_psi, int Mx, int My, int
    x fastest) into host_psi in the [Mx][My][Mz] layout.  dims/L may be NULL. */
 int xpfc_read_vtk(const char *path, double *host_psi, size_t cap, int dims[3], double L[3]);
 
+/* ---- allocation-free reduction ---------------------------------------------- */
+/* No counterpart in the reference.  The free energy of xpfc_FE_calc
+   (ff_factor times the sum of the FE_calc density) from five caller-owned
+   device arrays of n doubles, for callers that cannot allocate device memory
+   (inside a stream capture that must not grow a memory pool, or under a host
+   framework that owns all device memory).  Allocates nothing: its partial sums
+   live in a fixed 32 KB array in the library's device memory, which every GPU
+   that loads the library keeps until exit.  n is at most
+   XPFC_NOALLOC_MAX_POINTS (2^28; larger n returns XPFC_EINVAL).  stream is a
+   cudaStream_t (NULL: the legacy default stream); the call waits for its own
+   work and writes *F on the host.  The first call on each device looks up the
+   array's device address (cudaGetSymbolAddress) and must come before any
+   stream capture.  All calls share the array: calls that overlap on the GPU
+   race, so serialise them. */
+#define XPFC_NOALLOC_CHUNK 65536
+#define XPFC_NOALLOC_MAX_CHUNKS 4096
+#define XPFC_NOALLOC_MAX_POINTS ((long long)XPFC_NOALLOC_CHUNK * XPFC_NOALLOC_MAX_CHUNKS)
+int xpfc_FE_calc_noalloc(const double *psi, const double *psi2, const double *psi3, const double *psi4,
+                         const double *convl_r, long long n, double a, double b, double ff_factor,
+                         double *F, void *stream);
+
 /* ---- introspection ---------------------------------------------------------- */
 /* Kernel launches issued by this context since creation (all entry points). */
 long long xpfc_launch_count(const xpfc_ctx *ctx);

@@ -90,6 +90,8 @@ SIGNATURES = [
     ("xpfc_write_vtk", C.c_int, [C.c_char_p, _dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                  C.c_int]),
     ("xpfc_read_vtk", C.c_int, [C.c_char_p, _dp, C.c_size_t, C.POINTER(C.c_int), _dp]),
+    ("xpfc_FE_calc_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong,
+                                        C.c_double, C.c_double, C.c_double, _dp, C.c_void_p]),
     ("xpfc_launch_count", C.c_longlong, [_ctx]),
     ("xpfc_version", C.c_char_p, []),
 ]

@@ -31,6 +31,7 @@ def _units():
         ("launch_f64_p1.o", [nvcc()] + cu + ["-DXPFC_PART=1", "-c", os.path.join(CSRC, "xpfc_launch_f64.cu")]),
         ("launch_f64_p2.o", [nvcc()] + cu + ["-DXPFC_PART=2", "-c", os.path.join(CSRC, "xpfc_launch_f64.cu")]),
         ("capi.o", [nvcc()] + cu + ["-c", os.path.join(CSRC, "xpfc_capi.cu")]),
+        ("noalloc.o", [nvcc()] + cu + ["-c", os.path.join(CSRC, "xpfc_noalloc.cu")]),
         ("host.o", ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall",
                     "-c", os.path.join(CSRC, "xpfc_host.cpp")]),
     ]
