@@ -182,25 +182,16 @@ def run_ours(args):
 
     import xpfc_cuda_gb300 as X
 
+    from xpfc_cuda_gb300.replicas import Group
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    else:
-        dist = None
+    group = Group("nccl", device="cuda")
 
     def barrier():
-        if dist:
-            dist.barrier()
+        group.barrier()
         torch.cuda.synchronize()
 
-    def allmax(v):
-        if not dist:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    allmax = group.max
 
     n = args.size
     prec = X._lib.MIXED if args.precision == "mixed" else X._lib.FP64
@@ -235,7 +226,8 @@ def run_ours(args):
     prof = x.profile()
     x.set_profiling(False)
     ms_max = allmax(ms)
-    value = ws * n ** 3 * args.steps / (ms_max / 1e3) / 1e9
+    from xpfc_cuda_gb300.replicas import throughput
+    value = throughput(n ** 3 * args.steps, ms / 1e3, group) / 1e9
 
     # FP64 plain path on the same workload (the "vs FP64" half of the metric)
     fp64 = None
@@ -311,15 +303,14 @@ def run_ours(args):
                 "fp64": fp64}
         print(json.dumps(line), flush=True)
     x.close()
-    if dist:
-        dist.destroy_process_group()
+    group.close()
     return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="xpfc", choices=["xpfc", "reference"])
     ap.add_argument("--size", type=int, default=256)

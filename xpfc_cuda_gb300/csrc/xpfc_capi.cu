@@ -766,7 +766,7 @@ extern "C" int xpfc_set_profiling(xpfc_ctx *ctx, int enable) {
         ctx->prof_n[i] = 0;
     }
     if (ctx->profiling && ctx->ev_pool.empty()) {
-        ctx->ev_pool.resize(16384);
+        ctx->ev_pool.resize(65536);
         for (auto &e : ctx->ev_pool) XPFC_CUDA(ctx, cudaEventCreate(&e));
     }
     return XPFC_OK;

@@ -196,7 +196,8 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
     static constexpr int LINES = TX * NG;
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
-    static constexpr int MINB = 1;
+    // two resident blocks per SM (128 registers per thread) for the FP32 instances
+    static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256) ? 2 : 1;
 };
 
 // The update of one mode given its coefficients and noise (zero when off).
