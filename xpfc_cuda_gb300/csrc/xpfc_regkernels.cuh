@@ -15,6 +15,33 @@ __device__ __forceinline__ cplx<T> shfl_c(cplx<T> v, int src) {
     return mk<T>(__shfl_sync(FULLMASK, v.x, src), __shfl_sync(FULLMASK, v.y, src));
 }
 
+// Diagnostics sums: FP64 on the FP64 path; on the FP32 path compensated
+// (Kahan) FP32 within a thread and FP64 across threads, which keeps the sample
+// steps off GB300's narrow FP64 pipe.
+template <typename T, int NQ> struct DSum {
+    double v[NQ];
+    __device__ DSum() {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) v[q] = 0.0;
+    }
+    __device__ __forceinline__ void add(int q, double x) { v[q] += x; }
+    __device__ __forceinline__ double get(int q) const { return v[q]; }
+};
+template <int NQ> struct DSum<float, NQ> {
+    float s[NQ], c[NQ];
+    __device__ DSum() {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) s[q] = c[q] = 0.f;
+    }
+    __device__ __forceinline__ void add(int q, float x) {
+        const float y = x - c[q];
+        const float t = s[q] + y;
+        c[q] = (t - s[q]) - y;
+        s[q] = t;
+    }
+    __device__ __forceinline__ double get(int q) const { return (double)s[q] - (double)c[q]; }
+};
+
 // ---------------------------------------------------------------------------
 // column pass (C2C along a strided axis), TX columns per block
 // ---------------------------------------------------------------------------
@@ -152,7 +179,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
 #pragma unroll
         for (int j = 0; j < P; j++) v[j] = cscale(v[j], sc);
     } else if (MODE == ROW_FUSED || MODE == ROW_NL_FWD) {
-        double acc[NQ_ROW] = {0.0, 0.0, 0.0, 0.0};
+        DSum<T, NQ_ROW> acc;
         const T sc = (T)args.scale;
         const T a = (T)args.a, b = (T)args.b;
         T *rout = args.real_out ? reinterpret_cast<T *>(args.real_out) + row * (2 * N) : nullptr;
@@ -165,14 +192,23 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
             const T p20 = powi(x0, 2, args.ref_compat), p21 = powi(x1, 2, args.ref_compat);
             const T p30 = powi(x0, 3, args.ref_compat), p31 = powi(x1, 3, args.ref_compat);
             if (RED && valid) {
-                acc[0] += (double)x0 + (double)x1;
-                acc[1] += (double)p20 + (double)p21;
-                acc[2] += (double)p30 + (double)p31;
-                acc[3] += (double)powi(x0, 4, args.ref_compat) + (double)powi(x1, 4, args.ref_compat);
+                acc.add(0, x0);
+                acc.add(0, x1);
+                acc.add(1, p20);
+                acc.add(1, p21);
+                acc.add(2, p30);
+                acc.add(2, p31);
+                acc.add(3, powi(x0, 4, args.ref_compat));
+                acc.add(3, powi(x1, 4, args.ref_compat));
             }
             v[j] = mk<T>(-a * p20 + b * p30, -a * p21 + b * p31);
         }
-        if (RED) block_reduce_store<NQ_ROW>(acc, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
+        if (RED) {
+            double tot[NQ_ROW];
+#pragma unroll
+            for (int q = 0; q < NQ_ROW; q++) tot[q] = acc.get(q);
+            block_reduce_store<NQ_ROW>(tot, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
+        }
     }
     if (MODE != ROW_INV) {
         reg_fft<T, N, -1>(v, t, line, stw);
@@ -200,38 +236,53 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256) ? 2 : 1;
 };
 
+// k-space sums of one updated mode: weight c2 |X|^2 (free energy) and
+// weight |res|^2 (sse_calculation.cu:133-140).  On the FP32 path, with
+// Mo_res = Mo, the residual comes from the update itself,
+//   res = xi/dt + Mo k^2 ((1 - c2)(X - X') + eps X'),
+// where X - X' of two nearby FP32 values is exact; otherwise the general form
+// in FP64.
+template <typename T>
+__device__ __forceinline__ void diag_mode(const KSpace &ks, const Coef<T> &cf, cplx<T> xs, cplx<T> xw, cplx<T> noise,
+                                          cplx<T> xn, DSum<T, NQ_PEN> &acc, T weight) {
+    if constexpr (sizeof(T) == 4) {
+        if (ks.Mo_res == ks.Mo) {
+            const float m = ks.f_Mo * cf.k2, omc = 1.f - cf.c2, idt = 1.f / ks.f_dt;
+            const float rr = noise.x * idt + m * (omc * (xs.x - xn.x) + ks.f_eps * xn.x);
+            const float ri = noise.y * idt + m * (omc * (xs.y - xn.y) + ks.f_eps * xn.y);
+            acc.add(0, weight * cf.c2 * (xs.x * xs.x + xs.y * xs.y));
+            acc.add(1, weight * (rr * rr + ri * ri));
+            return;
+        }
+    }
+    const double xr = xs.x, xi = xs.y, k2 = cf.k2, c2 = cf.c2, w = weight;
+    const double rr = ((double)xn.x - xr) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xr + (double)xw.x);
+    const double ri = ((double)xn.y - xi) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xi + (double)xw.y);
+    acc.add(0, (T)(w * c2 * (xr * xr + xi * xi)));
+    acc.add(1, (T)(w * (rr * rr + ri * ri)));
+}
+
 // The update of one mode given its coefficients and noise (zero when off).
 // (interior modes: never k = 0, so no pinning)
 template <typename T, bool RED>
 __device__ __forceinline__ cplx<T> update_coef(const KSpace &ks, const Coef<T> &cf, cplx<T> xs, cplx<T> xw,
-                                               cplx<T> noise, double *acc, double weight) {
+                                               cplx<T> noise, DSum<T, NQ_PEN> &acc, T weight) {
     const cplx<T> num = cadd(xs, noise);
     cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
-    if (RED) {
-        const double xr = xs.x, xi = xs.y, k2 = cf.k2, c2 = cf.c2;
-        acc[0] += weight * c2 * (xr * xr + xi * xi);
-        const double rr = ((double)xn.x - xr) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xr + (double)xw.x);
-        const double ri = ((double)xn.y - xi) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xi + (double)xw.y);
-        acc[1] += weight * (rr * rr + ri * ri);
-    }
+    if (RED) diag_mode<T>(ks, cf, xs, xw, noise, xn, acc, weight);
     return xn;
 }
 
 template <typename T>
 __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const PenArgs &args, int i0, int i1, int i2,
-                                               cplx<T> xs, cplx<T> xw, double *acc, double weight) {
+                                               cplx<T> xs, cplx<T> xw, DSum<T, NQ_PEN> &acc, T weight) {
     const Coef<T> cf = kcoef<T>(ks, i0, i1, i2);
-    cplx<T> num = xs;
-    if (ks.noise_on) num = cadd(num, noise_at<T>(ks, i0, i1, i2, cf.k2));
+    cplx<T> noise = mk<T>((T)0, (T)0);
+    if (ks.noise_on) noise = noise_at<T>(ks, i0, i1, i2, cf.k2);
+    const cplx<T> num = cadd(xs, noise);
     cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
     if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)args.pin_value, (T)0);
-    if (args.want_red) {
-        const double xr = xs.x, xi = xs.y, k2 = cf.k2, c2 = cf.c2;
-        acc[0] += weight * c2 * (xr * xr + xi * xi);
-        const double rr = ((double)xn.x - xr) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xr + (double)xw.x);
-        const double ri = ((double)xn.y - xi) / ks.dt + ks.Mo_res * k2 * ((1.0 - c2) * xi + (double)xw.y);
-        acc[1] += weight * (rr * rr + ri * ri);
-    }
+    if (args.want_red) diag_mode<T>(ks, cf, xs, xw, noise, xn, acc, weight);
     return xn;
 }
 
@@ -269,7 +320,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     const int ln = g * TX + c;
     reg_fft2<T, N, -1>(vs, vw, t, bufS + ln * S::LP, bufW + ln * S::LP, stw);
 
-    double acc[NQ_PEN] = {0.0, 0.0};
+    DSum<T, NQ_PEN> acc;
     const T sc = (T)args.scale;
     const int nh = args.L0;
     const cplx<T> zero = mk<T>((T)0, (T)0);
@@ -302,8 +353,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const T h = (T)0.5;
             const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
             const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
-            const cplx<T> x0 = update_mode<T>(ks, args, 0, i1, i2, s0, w0, acc, 1.0);
-            const cplx<T> xN = update_mode<T>(ks, args, nh, i1, i2, sN, wN, acc, 1.0);
+            const cplx<T> x0 = update_mode<T>(ks, args, 0, i1, i2, s0, w0, acc, (T)1);
+            const cplx<T> xN = update_mode<T>(ks, args, nh, i1, i2, sN, wN, acc, (T)1);
             outS[gg * N + kz] = cscale(cadd(x0, cmuli<1>(xN)), sc);
         }
         __syncthreads();
@@ -324,12 +375,14 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const Coef<T> ca = kcoef<T>(ks, i0, i1a, i2a), cb = kcoef<T>(ks, i0, i1b, i2b);
             cplx<T> na = zero, nb = zero;
             if (ks.noise_on) noise_pair_interior<T>(ks, i0, i1a, i2a, ca.k2, cb.k2, na, nb);
-            vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, 2.0), sc);
-            vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, 2.0), sc);
+            vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, (T)2), sc);
+            vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, (T)2), sc);
         }
     }
-    if (RED)
-        block_reduce_store<NQ_PEN>(acc, args.partials + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * NQ_PEN, sred);
+    if (RED) {
+        double tot[NQ_PEN] = {acc.get(0), acc.get(1)};
+        block_reduce_store<NQ_PEN>(tot, args.partials + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * NQ_PEN, sred);
+    }
     if (!args.update) return;
     reg_fft<T, N, +1>(vs, t, bufS + ln * S::LP, stw);
     if (!valid) return;
