@@ -176,6 +176,57 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def sweep_cpu_estimate(params, steps, per_size_steps=3):
+    """Host-core time of the sweep, estimated from a few oracle steps per grid size."""
+    from oracle import oracle as O
+    t_step = {}
+    for N in sorted({p.Mx for p in params}):
+        L = N * DX
+        q = O.make_params(N, N, N, L=(L, L, L), a=1.0, b=1.0 / 3.0, sigma=0.3, peaks=FCC, envelope=1,
+                          ff_factor=DX ** 3)
+        psi = O.ic_noise(N, N, N, 0.04, 0.1, 1)
+        sec, _ = O.bench(q, psi, per_size_steps)
+        t_step[N] = sec / per_size_steps
+    total = sum(t_step[p.Mx] * steps for p in params)
+    return {"value": len(params) / total, "unit": "solves/s", "cores": O.threads(), "kind": "port",
+            "sample": "%d oracle steps per grid size (%s), scaled to %d instances x %d steps" % (
+                per_size_steps, ", ".join("%d^3: %.3f s/step" % (k, v) for k, v in sorted(t_step.items())),
+                len(params), steps)}
+
+
+def run_sweep(args, rank, local, group, barrier):
+    """Batched parameter sweep (xpfc_batch): solves/s through the C ABI."""
+    import numpy as np
+
+    from xpfc_cuda_gb300 import sweep as SW
+    ps = SW.sweep_params(args.sweep_n, seed=rank, device=local)
+    fields = SW.initial_fields(ps)
+    SW.solve_batch(ps, fields, 3)                    # warm-up: every kernel instance the sweep uses
+    barrier()
+    tb, (outs, diags, groups) = SW.timed(SW.solve_batch, ps, fields, args.sweep_steps)
+    barrier()
+    tb_max = group.max(tb)
+    solves = group.sum(len(ps)) / tb_max
+    out = {"value": solves, "unit": "solves/s", "instances": len(ps), "steps": args.sweep_steps,
+           "seconds": tb_max, "groups": groups,
+           "gpt_steps_per_s": group.sum(SW.points(ps) * args.sweep_steps) / tb_max / 1e9,
+           "finite": bool(all(np.isfinite(f).all() for f in outs)),
+           "workload": "N in U{48,64,96,128}^3, n0 in U[0,0.08], sigma in U[0.28,0.35], single-peak or fcc "
+                       "(p=0.5), dt=1, diagnostics every 100, FP32 bulk; seed i for instance i",
+           "timed": "xpfc_batch_create + initialize(host FP64 fields) + step + collect + get_field(host) + destroy"}
+    if not args.no_sweep_seq:
+        barrier()
+        ts, (outs_s, diags_s) = SW.timed(SW.solve_sequential, ps, fields, args.sweep_steps)
+        barrier()
+        out["sequential"] = {"value": group.sum(len(ps)) / group.max(ts), "unit": "solves/s", "seconds": ts,
+                             "what": "the same solves one xpfc_ctx after another"}
+        out["identical_to_sequential"] = bool(all(np.array_equal(a, b) for a, b in zip(outs, outs_s)) and
+                                             diags == diags_s)
+    if rank == 0 and group.world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = sweep_cpu_estimate(ps, args.sweep_steps)
+    return out
+
+
 def run_ours(args):
     import torch
     import numpy as np
@@ -294,13 +345,18 @@ def run_ours(args):
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(n)
 
+    sweep = None
+    if not args.no_sweep:
+        torch.cuda.set_stream(torch.cuda.default_stream())
+        sweep = run_sweep(args, rank, local, group, barrier)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == X._lib.MIXED else "f64",
                 "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, args.precision),
                 "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
-                "fp64": fp64}
+                "fp64": fp64, "sweep": sweep}
         print(json.dumps(line), flush=True)
     x.close()
     group.close()
@@ -319,6 +375,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-sweep-seq", action="store_true")
+    ap.add_argument("--sweep-n", type=int, default=64)
+    ap.add_argument("--sweep-steps", type=int, default=1000)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -198,6 +198,37 @@ int xpfc_write_vtk(const char *path, const double *host_psi, int Mx, int My, int
    x fastest) into host_psi in the [Mx][My][Mz] layout.  dims/L may be NULL. */
 int xpfc_read_vtk(const char *path, double *host_psi, size_t cap, int dims[3], double L[3]);
 
+/* ---- batched sweeps ---------------------------------------------------------- */
+/* No counterpart in the reference, which runs one solve per process (main.cu).
+   A batch advances n independent solves together.  Instances whose params
+   agree on everything but psi0, sigma, the peaks (npeaks, pk_*, envelope),
+   noise_seed and the initial-condition fields form one group; a group's fields
+   sit back to back in HBM and every pass of a step is one launch over all of
+   them (grid z = instance), so small grids fill the GPU.  Groups run
+   concurrently on their own streams (ps[0].stream, when set, serialises them).
+   Each instance gets the same results it would get alone in an xpfc_ctx with
+   the same params.  Instances need equal box lengths on every axis
+   (Lx = Ly (= Lz)): their coefficients come from per-instance shell tables. */
+typedef struct xpfc_batch xpfc_batch;
+int xpfc_batch_create(const xpfc_params *ps, int n, xpfc_batch **out);
+int xpfc_batch_destroy(xpfc_batch *b);
+const char *xpfc_batch_last_error(const xpfc_batch *b);
+int xpfc_batch_size(const xpfc_batch *b);                 /* n                      */
+int xpfc_batch_groups(const xpfc_batch *b);               /* groups formed          */
+int xpfc_batch_group_of(const xpfc_batch *b, int i);      /* group of instance i    */
+/* fields[i] (host, [Mx][My][Mz]) or NULL entries / a NULL array: the
+   instance's own generator, as xpfc_initialize(ctx, NULL).  Mean pinned to
+   each instance's psi0. */
+int xpfc_batch_initialize(xpfc_batch *b, const double *const *fields);
+/* nsteps more iterations of every instance, with the diagnostics schedule of
+   xpfc_step; returns when all groups are done.  _async only enqueues. */
+int xpfc_batch_step(xpfc_batch *b, long long nsteps);
+int xpfc_batch_step_async(xpfc_batch *b, long long nsteps);
+/* Waits for instance i's group; its diagnostics of the last step call
+   (XPFC_ENONFINITE when its F or mean is not finite). */
+int xpfc_batch_collect(xpfc_batch *b, int i, xpfc_diag *out, int cap, int *count);
+int xpfc_batch_get_field(xpfc_batch *b, int i, double *host_psi);
+
 /* ---- allocation-free reduction ---------------------------------------------- */
 /* No counterpart in the reference.  The free energy of xpfc_FE_calc
    (ff_factor times the sum of the FE_calc density) from five caller-owned

@@ -184,3 +184,16 @@ def test_extension_lines(tmp_path):
     p = X.read_input(str(tmp_path / "pfc.input"))
     assert p.Mz == 16 and p.Lz == 4.0 and p.precision == X._lib.MIXED and p.envelope == X._lib.ENVELOPE_MAX
     assert p.noise_amp == 0.01 and p.npeaks == 2 and p.pk_beta[1] == 6.0 and p.ref_compat == 0
+
+
+def test_batch_rejects_bad_input():
+    """xpfc_batch_create checks its arguments before touching a device."""
+    import xpfc_cuda_gb300 as X
+    with pytest.raises(X.XpfcError) as e:
+        X.Batch([])
+    assert e.value.status == X._lib.EINVAL
+    ok = X.default_params(Mx=32, My=32, Mz=32, Lx=4.0, Ly=4.0, Lz=4.0)
+    for bad in (dict(Lx=4.0, Ly=5.0), dict(Mx=31), dict(dt=0.0), dict(npeaks=0)):
+        with pytest.raises(X.XpfcError) as e:
+            X.Batch([ok, X.default_params(**dict(dict(Mx=32, My=32, Mz=32, Lx=4.0, Ly=4.0, Lz=4.0), **bad))])
+        assert e.value.status == X._lib.EINVAL, bad

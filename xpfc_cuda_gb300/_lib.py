@@ -90,6 +90,17 @@ SIGNATURES = [
     ("xpfc_write_vtk", C.c_int, [C.c_char_p, _dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                  C.c_int]),
     ("xpfc_read_vtk", C.c_int, [C.c_char_p, _dp, C.c_size_t, C.POINTER(C.c_int), _dp]),
+    ("xpfc_batch_create", C.c_int, [C.POINTER(XpfcParams), C.c_int, C.POINTER(C.c_void_p)]),
+    ("xpfc_batch_destroy", C.c_int, [C.c_void_p]),
+    ("xpfc_batch_last_error", C.c_char_p, [C.c_void_p]),
+    ("xpfc_batch_size", C.c_int, [C.c_void_p]),
+    ("xpfc_batch_groups", C.c_int, [C.c_void_p]),
+    ("xpfc_batch_group_of", C.c_int, [C.c_void_p, C.c_int]),
+    ("xpfc_batch_initialize", C.c_int, [C.c_void_p, C.POINTER(_dp)]),
+    ("xpfc_batch_step", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("xpfc_batch_step_async", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("xpfc_batch_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(XpfcDiag), C.c_int, C.POINTER(C.c_int)]),
+    ("xpfc_batch_get_field", C.c_int, [C.c_void_p, C.c_int, _dp]),
     ("xpfc_FE_calc_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong,
                                         C.c_double, C.c_double, C.c_double, _dp, C.c_void_p]),
     ("xpfc_launch_count", C.c_longlong, [_ctx]),

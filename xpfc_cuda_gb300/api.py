@@ -250,6 +250,98 @@ class Xpfc:
         return m.value
 
 
+def _records(recs, cnt):
+    return [dict(iteration=r.iteration, F=r.F if r.has & 1 else None, mean=r.mean if r.has & 1 else None,
+                 rms=r.rms if r.has & 2 else None) for r in recs[:cnt]]
+
+
+class Batch:
+    """n independent solves advanced together (an xpfc_batch): instances that
+    share grid, box and scheme constants form one group whose passes launch
+    once over all of its fields; groups run concurrently."""
+
+    def __init__(self, params_list):
+        self._L = _lib.load()
+        n = len(params_list)
+        arr = (XpfcParams * n)(*params_list)
+        h = C.c_void_p()
+        rc = self._L.xpfc_batch_create(arr, n, C.byref(h))
+        if rc != _lib.OK:
+            msg = self._L.xpfc_batch_last_error(None)
+            raise XpfcError(rc, msg.decode() if msg else "")
+        self._h = h
+        self.params = list(params_list)
+        self.n = n
+
+    def _c(self, rc):
+        if rc != _lib.OK:
+            msg = self._L.xpfc_batch_last_error(self._h)
+            raise XpfcError(rc, msg.decode() if msg else "")
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.xpfc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def groups(self):
+        return self._L.xpfc_batch_groups(self._h)
+
+    def group_of(self, i):
+        return self._L.xpfc_batch_group_of(self._h, i)
+
+    def initialize(self, fields=None):
+        """fields: None or a list of n host fields (None entries: the
+        instance's own generator); each mean is pinned to its psi0."""
+        if fields is None:
+            self._c(self._L.xpfc_batch_initialize(self._h, None))
+            return
+        keep = []
+        ptrs = (C.POINTER(C.c_double) * self.n)()
+        for i, f in enumerate(fields):
+            if f is None:
+                continue
+            p = self.params[i]
+            a = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+            if a.size != p.Mx * p.My * p.Mz:
+                raise ValueError("field %d has %d values, grid has %d" % (i, a.size, p.Mx * p.My * p.Mz))
+            keep.append(a)
+            ptrs[i] = _dp(a)
+        self._c(self._L.xpfc_batch_initialize(self._h, ptrs))
+
+    def step(self, nsteps):
+        self._c(self._L.xpfc_batch_step(self._h, nsteps))
+
+    def step_async(self, nsteps):
+        self._c(self._L.xpfc_batch_step_async(self._h, nsteps))
+
+    def collect(self, i, cap=64):
+        """Diagnostics of instance i from the last step call."""
+        recs = (XpfcDiag * cap)()
+        cnt = C.c_int(0)
+        self._c(self._L.xpfc_batch_collect(self._h, i, recs, cap, C.byref(cnt)))
+        return _records(recs, cnt.value)
+
+    def get_field(self, i):
+        p = self.params[i]
+        out = np.empty(p.Mx * p.My * p.Mz)
+        self._c(self._L.xpfc_batch_get_field(self._h, i, _dp(out)))
+        return out.reshape(p.Mx, p.My, p.Mz)
+
+
 def run_reference_loop(x, nsteps, t_sample):
     """main.cu:232-450 through the staged wrappers (FP64, reference order).
 

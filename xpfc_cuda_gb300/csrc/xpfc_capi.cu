@@ -45,6 +45,7 @@ struct xpfc_ctx {
     size_t hstage_bytes = 0;
     // diagnostics schedule of the last step call
     std::vector<long long> diag_its;
+    std::map<long long, int> diag_slot;   // iteration -> slot
     long long diag_it0 = 0, diag_fin = 0;
     bool diag_final = false, diag_pending = false;
     // per-pass profiling with CUDA events
@@ -53,6 +54,16 @@ struct xpfc_ctx {
     std::vector<std::pair<int, int>> ev_used;   // (pass, pool index of the start event)
     double prof_ms[8] = {0};
     long long prof_n[8] = {0};
+    // batched instances (one field: nb = 1).  Instance i's field sits i
+    // fields of ncells values after S (and W), its coefficient table i tables
+    // of mmax + 1 shells after the first, its sums and slots after the other
+    // instances'.  Per instance: params in inst[i] (psi0, peaks, seeds).
+    int nb = 1;
+    std::vector<xpfc_params> inst;
+    double *pin_values = nullptr;          // psi0_i * ncells
+    unsigned long long *seeds = nullptr;   // noise_seed_i
+    long long zstride = 0;                 // complex elements between instances
+    size_t part_per_inst = 0;              // partial-sum doubles per instance
 };
 
 enum { PASS_PENCIL = 0, PASS_COL_INV = 1, PASS_ROW = 2, PASS_COL_FWD = 3, PASS_RED = 4 };
@@ -236,6 +247,8 @@ static KSpace make_kspace(const xpfc_ctx *ctx, bool dbl) {
     ks.dk1sq = d1 * d1;
     ks.dk2sq = ctx->n2 > 1 ? d2 * d2 : 0.0;
     ks.table = dbl ? ctx->table_d : ctx->table_f;
+    ks.tstride = ctx->nb > 1 ? (long long)ctx->mmax + 1 : 0;
+    ks.seeds = ctx->nb > 1 ? ctx->seeds : nullptr;
     ks.mmax = ctx->mmax;
     ks.dt = p.dt;
     ks.Mo = p.Mo;
@@ -275,20 +288,23 @@ static int build_tables(xpfc_ctx *ctx) {
     const int h0 = ctx->n0 / 2, h1 = ctx->n1 / 2, h2 = ctx->n2 / 2;
     ctx->mmax = h0 * h0 + h1 * h1 + h2 * h2;
     const size_t nm = (size_t)ctx->mmax + 1;
-    std::vector<double> td(4 * nm);
-    std::vector<float> tf(4 * nm);
+    std::vector<double> td(4 * nm * ctx->nb);
+    std::vector<float> tf(4 * nm * ctx->nb);
     const double dk = 2.0 * M_PI / ctx->Lax[0];
-    const xpfc_params &p = ctx->p;
-    for (size_t m = 0; m < nm; m++) {
-        const double k2 = dk * dk * (double)m;
-        const double c2 = c2_of(p, std::sqrt(k2));
-        const double den = (1.0 + k2 * p.dt * p.Mo * (1.0 - p.eps) - k2 * p.Mo * p.dt * c2);
-        td[4 * m + 0] = 1.0 / den;
-        td[4 * m + 1] = -(k2 * p.Mo * p.dt) / den;
-        td[4 * m + 2] = c2;
-        td[4 * m + 3] = k2;
-        for (int j = 0; j < 4; j++) tf[4 * m + j] = (float)td[4 * m + j];
+    for (int i = 0; i < ctx->nb; i++) {
+        const xpfc_params &p = ctx->inst[i];
+        double *d = td.data() + 4 * nm * i;
+        for (size_t m = 0; m < nm; m++) {
+            const double k2 = dk * dk * (double)m;
+            const double c2 = c2_of(p, std::sqrt(k2));
+            const double den = (1.0 + k2 * p.dt * p.Mo * (1.0 - p.eps) - k2 * p.Mo * p.dt * c2);
+            d[4 * m + 0] = 1.0 / den;
+            d[4 * m + 1] = -(k2 * p.Mo * p.dt) / den;
+            d[4 * m + 2] = c2;
+            d[4 * m + 3] = k2;
+        }
     }
+    for (size_t j = 0; j < td.size(); j++) tf[j] = (float)td[j];
     XPFC_CUDA(ctx, cudaMalloc(&ctx->table_d, sizeof(double) * td.size()));
     XPFC_CUDA(ctx, cudaMalloc(&ctx->table_f, sizeof(float) * tf.size()));
     XPFC_CUDA(ctx, cudaMemcpy(ctx->table_d, td.data(), sizeof(double) * td.size(), cudaMemcpyHostToDevice));
@@ -305,15 +321,38 @@ static int ensure_partials(xpfc_ctx *ctx, size_t n) {
     return XPFC_OK;
 }
 
-extern "C" int xpfc_create(const xpfc_params *p, xpfc_ctx **out) {
-    if (!p || !out) return fail(nullptr, XPFC_EINVAL, "null argument");
-    *out = nullptr;
-    if (p->Mx <= 0 || p->My <= 0 || p->Mz <= 0) return fail(nullptr, XPFC_EINVAL, "grid sizes must be positive");
-    if (p->dt <= 0.0 || p->npeaks < 1 || p->npeaks > XPFC_MAX_PEAKS)
+// A context over nb instances that share everything but psi0, the peaks
+// (sigma, envelope) and the seeds: ps[0..nb-1].  nb = 1 is xpfc_create.
+// The checks that need no device: sizes, scheme constants, compiled lengths.
+static int check_params(const xpfc_params *q) {
+    if (q->Mx <= 0 || q->My <= 0 || q->Mz <= 0) return fail(nullptr, XPFC_EINVAL, "grid sizes must be positive");
+    if (q->dt <= 0.0 || q->npeaks < 1 || q->npeaks > XPFC_MAX_PEAKS)
         return fail(nullptr, XPFC_EINVAL, "dt must be > 0 and 1 <= npeaks <= 8");
-    if (p->precision != XPFC_FP64 && p->precision != XPFC_MIXED) return fail(nullptr, XPFC_EINVAL, "bad precision");
+    if (q->precision != XPFC_FP64 && q->precision != XPFC_MIXED) return fail(nullptr, XPFC_EINVAL, "bad precision");
+    const bool three = q->Mz > 1;
+    const int n0 = three ? q->Mz : q->My, n1 = three ? q->My : q->Mx, n2 = three ? q->Mx : 1;
+    if (n0 % 2 != 0 || n1 % 2 != 0 || (three && n2 % 2 != 0))
+        return fail(nullptr, XPFC_EINVAL, "grid sizes must be even");
+    if (!row_supported(n0 / 2))
+        return fail(nullptr, XPFC_EINVAL, "unsupported size of the fastest axis: " + std::to_string(n0));
+    if (!col_supported(n1)) return fail(nullptr, XPFC_EINVAL, "unsupported axis length " + std::to_string(n1));
+    if (three && (!col_supported(n2) || !pen_supported(n2, 2)))
+        return fail(nullptr, XPFC_EINVAL, "unsupported axis length " + std::to_string(n2));
+    if (!three && !pen_supported(n1, 1))
+        return fail(nullptr, XPFC_EINVAL, "unsupported axis length " + std::to_string(n1));
+    return XPFC_OK;
+}
+
+static int create_group(const xpfc_params *ps, int nb, xpfc_ctx **out) {
+    const xpfc_params *p = ps;
+    for (int i = 0; i < nb; i++) {
+        const int rc = check_params(ps + i);
+        if (rc != XPFC_OK) return rc;
+    }
     xpfc_ctx *ctx = new xpfc_ctx();
     ctx->p = *p;
+    ctx->nb = nb;
+    ctx->inst.assign(ps, ps + nb);
     ctx->three_d = p->Mz > 1;
     if (ctx->three_d) {
         ctx->n0 = p->Mz; ctx->n1 = p->My; ctx->n2 = p->Mx;
@@ -324,18 +363,7 @@ extern "C" int xpfc_create(const xpfc_params *p, xpfc_ctx **out) {
     }
     ctx->L0 = ctx->n0 / 2;
     ctx->ncells = (long long)ctx->n0 * ctx->n1 * ctx->n2;
-    auto reject = [&](const std::string &m) {
-        set_thread_error(m);
-        delete ctx;
-        return XPFC_EINVAL;
-    };
-    if (ctx->n0 % 2 != 0 || ctx->n1 % 2 != 0 || (ctx->three_d && ctx->n2 % 2 != 0))
-        return reject("grid sizes must be even");
-    if (!row_supported(ctx->L0)) return reject("unsupported size of the fastest axis: " + std::to_string(ctx->n0));
-    if (!col_supported(ctx->n1)) return reject("unsupported axis length " + std::to_string(ctx->n1));
-    if (ctx->three_d && (!col_supported(ctx->n2) || !pen_supported(ctx->n2, 2)))
-        return reject("unsupported axis length " + std::to_string(ctx->n2));
-    if (!ctx->three_d && !pen_supported(ctx->n1, 1)) return reject("unsupported axis length " + std::to_string(ctx->n1));
+    ctx->zstride = nb > 1 ? ctx->ncells / 2 : 0;
     cudaError_t e = cudaSetDevice(p->device);
     if (e != cudaSuccess) {
         set_thread_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
@@ -354,7 +382,7 @@ extern "C" int xpfc_create(const xpfc_params *p, xpfc_ctx **out) {
         ctx->own_stream = true;
     }
     ctx->esz = p->precision == XPFC_MIXED ? sizeof(float) : sizeof(double);
-    const size_t bytes = ctx->esz * (size_t)ctx->ncells;
+    const size_t bytes = ctx->esz * (size_t)ctx->ncells * nb;
     int rc = XPFC_OK;
     if (cudaMalloc(&ctx->S, bytes) != cudaSuccess || cudaMalloc(&ctx->W, bytes) != cudaSuccess) {
         set_thread_error("device allocation of the state failed");
@@ -368,11 +396,24 @@ extern "C" int xpfc_create(const xpfc_params *p, xpfc_ctx **out) {
         const int tx = ctx->esz == 4 ? (ctx->three_d ? pen_tx<float>(ctx->n2, 2) : pen_tx<float>(ctx->n1, 1))
                                      : (ctx->three_d ? pen_tx<double>(ctx->n2, 2) : pen_tx<double>(ctx->n1, 1));
         const size_t penblk = (size_t)(L0 / tx + 1) * (ctx->n1 / 2 + 1);
-        size_t need = std::max(rowblk * NQ_ROW, penblk * NQ_PEN);
-        need = std::max(need, (size_t)DENSITY_BLOCKS);
+        ctx->part_per_inst = std::max(rowblk * NQ_ROW, penblk * NQ_PEN);
+        const size_t need = std::max(ctx->part_per_inst * nb, (size_t)DENSITY_BLOCKS);
         rc = ensure_partials(ctx, need);
     }
-    if (rc == XPFC_OK && cudaMalloc(&ctx->init_red, sizeof(double) * 8) != cudaSuccess) rc = XPFC_ENOMEM;
+    if (rc == XPFC_OK && cudaMalloc(&ctx->init_red, sizeof(double) * 8 * nb) != cudaSuccess) rc = XPFC_ENOMEM;
+    if (rc == XPFC_OK && nb > 1) {
+        std::vector<double> pv(nb);
+        std::vector<unsigned long long> sd(nb);
+        for (int i = 0; i < nb; i++) {
+            pv[i] = ps[i].psi0 * (double)ctx->ncells;
+            sd[i] = ps[i].noise_seed;
+        }
+        if (cudaMalloc(&ctx->pin_values, sizeof(double) * nb) != cudaSuccess ||
+            cudaMalloc(&ctx->seeds, sizeof(unsigned long long) * nb) != cudaSuccess ||
+            cudaMemcpy(ctx->pin_values, pv.data(), sizeof(double) * nb, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(ctx->seeds, sd.data(), sizeof(unsigned long long) * nb, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = XPFC_ENOMEM;
+    }
     if (rc != XPFC_OK) {
         set_thread_error(ctx->err.empty() ? "context set-up failed" : ctx->err);
         xpfc_destroy(ctx);
@@ -380,6 +421,12 @@ extern "C" int xpfc_create(const xpfc_params *p, xpfc_ctx **out) {
     }
     *out = ctx;
     return XPFC_OK;
+}
+
+extern "C" int xpfc_create(const xpfc_params *p, xpfc_ctx **out) {
+    if (!p || !out) return fail(nullptr, XPFC_EINVAL, "null argument");
+    *out = nullptr;
+    return create_group(p, 1, out);
 }
 
 extern "C" int xpfc_destroy(xpfc_ctx *ctx) {
@@ -395,6 +442,8 @@ extern "C" int xpfc_destroy(xpfc_ctx *ctx) {
     cudaFree(ctx->partials);
     cudaFree(ctx->slots);
     cudaFree(ctx->init_red);
+    cudaFree(ctx->pin_values);
+    cudaFree(ctx->seeds);
     if (ctx->hslots) cudaFreeHost(ctx->hslots);
     if (ctx->hstage) cudaFreeHost(ctx->hstage);
     for (int b = 0; b < XPFC_NBUF; b++) cudaFree(ctx->staged[b]);
@@ -438,6 +487,8 @@ static int fft_forward_xy(xpfc_ctx *ctx, void *buf, bool do_rows) {
         ra.out = buf;
         ra.nrows = (long long)ctx->n1 * ctx->n2;
         ra.scale = 1.0;
+        ra.zstride = ctx->zstride;
+        ra.nz = ctx->nb;
         XPFC_LAUNCH(ctx, launch_row<T>(ROW_FWD, ctx->L0, ra, tw0, tw2, ctx->stream, nullptr));
     }
     if (!ctx->three_d) return XPFC_OK;
@@ -448,6 +499,8 @@ static int fft_forward_xy(xpfc_ctx *ctx, void *buf, bool do_rows) {
     ca.ostride = (long long)ctx->n1 * ctx->L0;
     ca.scale = 1.0;
     ca.ncols = ctx->L0;
+    ca.zstride = ctx->zstride;
+    ca.nz = ctx->nb;
     XPFC_LAUNCH(ctx, launch_col<T>(-1, ctx->n1, ca, ctx->n2, tw1, ctx->stream));
     return XPFC_OK;
 }
@@ -495,7 +548,7 @@ static int fft_full(xpfc_ctx *ctx, void *buf, int dir) {
 template <typename T>
 static int init_fused(xpfc_ctx *ctx, const double *dpsi) {
     const bool dbl = sizeof(T) == 8;
-    const long long n = ctx->ncells;
+    const long long n = ctx->ncells * ctx->nb;
     if (dbl) XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->S, dpsi, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     else XPFC_LAUNCH(ctx, launch_convert_d2f(dpsi, (float *)ctx->S, n, ctx->stream));
     void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl);
@@ -511,9 +564,11 @@ static int init_fused(xpfc_ctx *ctx, const double *dpsi) {
     ra.partials = ctx->partials;
     ra.want_red = 1;
     ra.ref_compat = ctx->p.ref_compat;
+    ra.zstride = ctx->zstride;
+    ra.nz = ctx->nb;
     int nb = 0;
     XPFC_LAUNCH(ctx, launch_row<T>(ROW_NL_FWD, ctx->L0, ra, tw0, tw2, ctx->stream, &nb));
-    XPFC_LAUNCH(ctx, launch_finalize(NQ_ROW, ctx->partials, nb, ctx->init_red, ctx->stream));
+    XPFC_LAUNCH(ctx, launch_finalize(NQ_ROW, ctx->partials, nb, ctx->init_red, ctx->stream, ctx->nb, 8));
     int rc = fft_forward_xy<T>(ctx, ctx->S, true);
     if (rc != XPFC_OK) return rc;
     if (ctx->three_d) {
@@ -572,6 +627,9 @@ static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int wan
     pa.partials = ctx->partials;
     pa.pin = (!dbl) ? 1 : 0;
     pa.pin_value = ctx->p.psi0 * (double)ctx->ncells;
+    pa.pin_values = ctx->nb > 1 ? ctx->pin_values : nullptr;
+    pa.zstride = ctx->zstride;
+    pa.nz = ctx->nb;
     const int npairs = ctx->three_d ? ctx->n1 / 2 + 1 : 1;
     ProfScope ps(ctx, PASS_PENCIL);
     XPFC_LAUNCH(ctx, launch_pencil<T>(Lp, ctx->three_d ? 2 : 1, pa, ks, npairs, twp, ctx->stream, nb));
@@ -590,6 +648,8 @@ static int launch_xy_pass(xpfc_ctx *ctx, int want_red, int *nb) {
     ra.partials = ctx->partials;
     ra.want_red = want_red;
     ra.ref_compat = ctx->p.ref_compat;
+    ra.zstride = ctx->zstride;
+    ra.nz = ctx->nb;
     if (ctx->three_d) {
         void *tw1 = twiddle(ctx, ctx->n1, dbl);
         if (!tw1) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
@@ -600,6 +660,8 @@ static int launch_xy_pass(xpfc_ctx *ctx, int want_red, int *nb) {
         cy.ostride = (long long)ctx->n1 * ctx->L0;
         cy.scale = 1.0;
         cy.ncols = ctx->L0;
+        cy.zstride = ctx->zstride;
+        cy.nz = ctx->nb;
         {
             ProfScope ps(ctx, PASS_COL_INV);
             XPFC_LAUNCH(ctx, launch_col<T>(1, ctx->n1, cy, ctx->n2, tw1, ctx->stream));
@@ -636,9 +698,10 @@ static bool diag_wantR(const xpfc_ctx *ctx, long long i) {
     return i < ctx->diag_fin && ts > 0 && i % ts == 0;
 }
 
-// Enqueues nsteps iterations with their diagnostics into device slots.
-template <typename T>
-static int fused_enqueue(xpfc_ctx *ctx, long long nsteps, bool final_F) {
+// A step call in three parts, so that a batch can interleave its groups:
+// begin (diagnostics schedule and slots), the iterations [i0, i1), end
+// (final free energy, copy of the slots to the host).
+static int enqueue_begin(xpfc_ctx *ctx, long long nsteps, bool final_F) {
     const long long it0 = ctx->iteration, fin = it0 + nsteps;
     const int ts = ctx->p.t_sample;
     ctx->diag_it0 = it0;
@@ -646,7 +709,8 @@ static int fused_enqueue(xpfc_ctx *ctx, long long nsteps, bool final_F) {
     ctx->diag_final = final_F;
     std::vector<long long> &its = ctx->diag_its;
     its.clear();
-    std::map<long long, int> slot;
+    std::map<long long, int> &slot = ctx->diag_slot;
+    slot.clear();
     auto add = [&](long long i) {
         if (!slot.count(i)) {
             slot[i] = (int)its.size();
@@ -658,64 +722,99 @@ static int fused_enqueue(xpfc_ctx *ctx, long long nsteps, bool final_F) {
         for (long long i = ((it0 / ts) + 1) * ts; i <= fin; i += ts)
             if (diag_wantF(ctx, i) || diag_wantR(ctx, i)) add(i);
     if (final_F) add(fin);
+    // slots: [instance][diagnostics iteration][8]
     const int ns = (int)its.size();
-    if (ns > ctx->slots_cap) {
+    const int nbi = ctx->nb;
+    const long long sstride = 8LL * ns;
+    if (ns * nbi > ctx->slots_cap) {
         cudaFree(ctx->slots);
         if (ctx->hslots) cudaFreeHost(ctx->hslots);
         ctx->slots = nullptr;
         ctx->hslots = nullptr;
-        XPFC_CUDA(ctx, cudaMalloc(&ctx->slots, sizeof(double) * 8 * ns));
-        XPFC_CUDA(ctx, cudaMallocHost(&ctx->hslots, sizeof(double) * 8 * ns));
-        ctx->slots_cap = ns;
+        ctx->slots_cap = 0;
+        XPFC_CUDA(ctx, cudaMalloc(&ctx->slots, sizeof(double) * 8 * ns * nbi));
+        XPFC_CUDA(ctx, cudaMallocHost(&ctx->hslots, sizeof(double) * 8 * ns * nbi));
+        ctx->slots_cap = ns * nbi;
     }
-    if (ns > 0) XPFC_CUDA(ctx, cudaMemsetAsync(ctx->slots, 0, sizeof(double) * 8 * ns, ctx->stream));
+    if (ns > 0) XPFC_CUDA(ctx, cudaMemsetAsync(ctx->slots, 0, sizeof(double) * 8 * ns * nbi, ctx->stream));
     if (it0 == 0 && slot.count(0))
-        XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->slots + 8 * slot[0], ctx->init_red, sizeof(double) * NQ_ROW,
-                                       cudaMemcpyDeviceToDevice, ctx->stream));
-    for (long long i = it0; i < fin; i++) {
+        XPFC_CUDA(ctx, cudaMemcpy2DAsync(ctx->slots + 8 * slot[0], sizeof(double) * sstride, ctx->init_red,
+                                         sizeof(double) * 8, sizeof(double) * NQ_ROW, nbi, cudaMemcpyDeviceToDevice,
+                                         ctx->stream));
+    return XPFC_OK;
+}
+
+template <typename T>
+static int enqueue_steps(xpfc_ctx *ctx, long long i0, long long i1) {
+    std::map<long long, int> &slot = ctx->diag_slot;
+    const int nbi = ctx->nb;
+    const long long sstride = 8LL * (long long)ctx->diag_its.size();
+    for (long long i = i0; i < i1; i++) {
         const bool red = diag_wantF(ctx, i) || diag_wantR(ctx, i);
         int nb = 0;
         int rc = launch_pencil_pass<T>(ctx, i, 1, red ? 1 : 0, &nb);
         if (rc != XPFC_OK) return rc;
         if (red) {
             ProfScope ps(ctx, PASS_RED);
-            XPFC_LAUNCH(ctx, launch_finalize(NQ_PEN, ctx->partials, nb, ctx->slots + 8 * slot[i] + 4, ctx->stream));
+            XPFC_LAUNCH(ctx, launch_finalize(NQ_PEN, ctx->partials, nb, ctx->slots + 8 * slot[i] + 4, ctx->stream, nbi,
+                                             sstride));
         }
         const bool redl = diag_wantF(ctx, i + 1);
         rc = launch_xy_pass<T>(ctx, redl ? 1 : 0, &nb);
         if (rc != XPFC_OK) return rc;
         if (redl) {
             ProfScope ps(ctx, PASS_RED);
-            XPFC_LAUNCH(ctx, launch_finalize(NQ_ROW, ctx->partials, nb, ctx->slots + 8 * slot[i + 1], ctx->stream));
+            XPFC_LAUNCH(ctx, launch_finalize(NQ_ROW, ctx->partials, nb, ctx->slots + 8 * slot[i + 1], ctx->stream, nbi,
+                                             sstride));
         }
     }
-    if (final_F && diag_wantF(ctx, fin)) {
+    return XPFC_OK;
+}
+
+template <typename T>
+static int enqueue_end(xpfc_ctx *ctx) {
+    std::map<long long, int> &slot = ctx->diag_slot;
+    const long long fin = ctx->diag_fin;
+    const int ns = (int)ctx->diag_its.size();
+    const int nbi = ctx->nb;
+    const long long sstride = 8LL * ns;
+    if (ctx->diag_final && diag_wantF(ctx, fin)) {
         // the final state's nonlocal term needs its spectrum: diagnostics-only pencil pass
         int nb = 0;
         int rc = launch_pencil_pass<T>(ctx, fin, 0, 1, &nb);
         if (rc != XPFC_OK) return rc;
-        XPFC_LAUNCH(ctx, launch_finalize(NQ_PEN, ctx->partials, nb, ctx->slots + 8 * slot[fin] + 4, ctx->stream));
+        XPFC_LAUNCH(ctx, launch_finalize(NQ_PEN, ctx->partials, nb, ctx->slots + 8 * slot[fin] + 4, ctx->stream, nbi,
+                                         sstride));
     }
     if (ns > 0)
-        XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->hslots, ctx->slots, sizeof(double) * 8 * ns, cudaMemcpyDeviceToHost,
-                                       ctx->stream));
+        XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->hslots, ctx->slots, sizeof(double) * 8 * ns * nbi,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
     ctx->iteration = fin;
     ctx->diag_pending = true;
     return XPFC_OK;
 }
 
-extern "C" int xpfc_collect(xpfc_ctx *ctx, xpfc_diag *out, int cap, int *count) {
-    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
-    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+// Enqueues nsteps iterations with their diagnostics into device slots.
+template <typename T>
+static int fused_enqueue(xpfc_ctx *ctx, long long nsteps, bool final_F) {
+    int rc = enqueue_begin(ctx, nsteps, final_F);
+    if (rc == XPFC_OK) rc = enqueue_steps<T>(ctx, ctx->diag_it0, ctx->diag_fin);
+    if (rc == XPFC_OK) rc = enqueue_end<T>(ctx);
+    return rc;
+}
+
+// Diagnostics of instance k from the last step call (stream already synchronised).
+static int collect_inst(xpfc_ctx *ctx, int k, xpfc_diag *out, int cap, int *count) {
     if (count) *count = 0;
     if (!ctx->diag_pending) return XPFC_OK;
-    const xpfc_params &p = ctx->p;
+    const xpfc_params &p = ctx->inst[k];
     const double N = (double)ctx->ncells;
+    const size_t ns = ctx->diag_its.size();
     int produced = 0;
     bool nonfinite = false;
-    for (size_t s = 0; s < ctx->diag_its.size(); s++) {
+    for (size_t s = 0; s < ns; s++) {
         const long long i = ctx->diag_its[s];
-        const double *v = ctx->hslots + 8 * s;
+        const double *v = ctx->hslots + 8 * (ns * k + s);
         xpfc_diag d;
         d.iteration = i;
         d.has = 0;
@@ -737,6 +836,12 @@ extern "C" int xpfc_collect(xpfc_ctx *ctx, xpfc_diag *out, int cap, int *count) 
     if (count) *count = (!out || produced < cap) ? produced : cap;
     if (nonfinite) return fail(ctx, XPFC_ENONFINITE, "free energy or mean is not finite");
     return XPFC_OK;
+}
+
+extern "C" int xpfc_collect(xpfc_ctx *ctx, xpfc_diag *out, int cap, int *count) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return collect_inst(ctx, 0, out, cap, count);
 }
 
 extern "C" int xpfc_step(xpfc_ctx *ctx, long long nsteps, xpfc_diag *out, int cap, int *count) {
@@ -781,8 +886,9 @@ extern "C" int xpfc_get_profile(xpfc_ctx *ctx, int pass, double *ms, long long *
 }
 
 template <typename T>
-static int field_to_X(xpfc_ctx *ctx) {
+static int field_to_X(xpfc_ctx *ctx, int k = 0) {
     const bool dbl = sizeof(T) == 8;
+    void *Sk = (char *)ctx->S + ctx->esz * (size_t)ctx->ncells * k;
     if (!ctx->X) XPFC_CUDA(ctx, cudaMalloc(&ctx->X, ctx->esz * (size_t)ctx->ncells));
     void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl);
     if (!tw0 || !tw2) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
@@ -792,7 +898,7 @@ static int field_to_X(xpfc_ctx *ctx) {
     if (ctx->three_d) {
         void *tw1 = twiddle(ctx, ctx->n1, dbl);
         ColArgs cy{};
-        cy.in = ctx->S;
+        cy.in = Sk;
         cy.out = ctx->X;
         cy.es = ctx->L0;
         cy.ostride = (long long)ctx->n1 * ctx->L0;
@@ -802,7 +908,7 @@ static int field_to_X(xpfc_ctx *ctx) {
         ra.in = ctx->X;
         ra.scale = 1.0 / ((double)ctx->n0 * ctx->n1);
     } else {
-        ra.in = ctx->S;
+        ra.in = Sk;
         ra.scale = 1.0 / (double)ctx->n0;
     }
     XPFC_LAUNCH(ctx, launch_row<T>(ROW_INV, ctx->L0, ra, tw0, tw2, ctx->stream, nullptr));
@@ -1012,5 +1118,207 @@ extern "C" int xpfc_sse_calculation(xpfc_ctx *ctx, int n, int psi_kp1, int psi_k
     rc = reduce_sum(ctx, res, nullptr, nullptr, nullptr, nullptr, 1, &s);
     if (rc != XPFC_OK) return rc;
     *rms = std::sqrt(s / (double)ctx->ncells);   // sum_reduction.cu:77
+    return XPFC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched sweeps: groups of instances that differ only in psi0, peaks, seeds
+// and initial fields share one context whose launches cover all of them
+// ---------------------------------------------------------------------------
+struct xpfc_batch {
+    std::vector<xpfc_ctx *> groups;
+    std::vector<std::pair<int, int>> where;   // instance -> (group, index in group)
+    std::string err;
+};
+
+static int bfail(xpfc_batch *b, int code, const std::string &m) {
+    if (b) b->err = m;
+    else set_thread_error(m);
+    return code;
+}
+
+// params that must agree within a group
+static bool same_group(const xpfc_params &a, const xpfc_params &b) {
+    return a.Mx == b.Mx && a.My == b.My && a.Mz == b.Mz && a.Lx == b.Lx && a.Ly == b.Ly && a.Lz == b.Lz &&
+           a.a == b.a && a.b == b.b && a.eps == b.eps && a.Mo == b.Mo && a.dt == b.dt && a.t_sample == b.t_sample &&
+           a.precision == b.precision && a.ref_compat == b.ref_compat && a.noise_amp == b.noise_amp &&
+           a.device == b.device && a.stream == b.stream;
+}
+
+extern "C" int xpfc_batch_create(const xpfc_params *ps, int n, xpfc_batch **out) {
+    if (!ps || !out || n < 1) return bfail(nullptr, XPFC_EINVAL, "null argument or n < 1");
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        const xpfc_params &p = ps[i];
+        const bool cubic = p.Lx == p.Ly && (p.Mz == 1 || p.Lx == p.Lz);
+        if (!cubic) return bfail(nullptr, XPFC_EINVAL, "batched instances need equal box lengths on every axis");
+        if (check_params(&p) != XPFC_OK)
+            return bfail(nullptr, XPFC_EINVAL, "instance " + std::to_string(i) + ": " + thread_error());
+    }
+    // group by shared params, in order of first appearance
+    std::vector<std::vector<int>> members;
+    std::vector<int> gid(n, -1);
+    for (int i = 0; i < n; i++) {
+        for (size_t g = 0; g < members.size() && gid[i] < 0; g++)
+            if (same_group(ps[members[g][0]], ps[i])) gid[i] = (int)g;
+        if (gid[i] < 0) {
+            gid[i] = (int)members.size();
+            members.emplace_back();
+        }
+        members[gid[i]].push_back(i);
+    }
+    xpfc_batch *b = new xpfc_batch();
+    b->where.resize(n);
+    for (size_t g = 0; g < members.size(); g++) {
+        std::vector<xpfc_params> gp;
+        for (size_t k = 0; k < members[g].size(); k++) {
+            gp.push_back(ps[members[g][k]]);
+            b->where[members[g][k]] = {(int)g, (int)k};
+        }
+        xpfc_ctx *ctx = nullptr;
+        const int rc = create_group(gp.data(), (int)gp.size(), &ctx);
+        if (rc != XPFC_OK) {
+            const std::string m = thread_error();
+            xpfc_batch_destroy(b);
+            return bfail(nullptr, rc, "group " + std::to_string(g) + ": " + m);
+        }
+        b->groups.push_back(ctx);
+    }
+    *out = b;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_batch_destroy(xpfc_batch *b) {
+    if (!b) return XPFC_OK;
+    for (xpfc_ctx *c : b->groups) xpfc_destroy(c);
+    delete b;
+    return XPFC_OK;
+}
+
+extern "C" const char *xpfc_batch_last_error(const xpfc_batch *b) { return b ? b->err.c_str() : thread_error(); }
+extern "C" int xpfc_batch_size(const xpfc_batch *b) { return b ? (int)b->where.size() : 0; }
+extern "C" int xpfc_batch_groups(const xpfc_batch *b) { return b ? (int)b->groups.size() : 0; }
+extern "C" int xpfc_batch_group_of(const xpfc_batch *b, int i) {
+    return (b && i >= 0 && i < (int)b->where.size()) ? b->where[i].first : -1;
+}
+
+static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) {
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    const size_t n = (size_t)ctx->ncells, nb = (size_t)ctx->nb;
+    int rc = host_stage(ctx, sizeof(double) * n * nb);
+    if (rc != XPFC_OK) return rc;
+    double *h = (double *)ctx->hstage;
+    for (size_t k = 0; k < nb; k++) {
+        if (fields[k]) {
+            memcpy(h + k * n, fields[k], sizeof(double) * n);
+            pin_mean(h + k * n, n, ctx->inst[k].psi0);
+        } else {
+            rc = build_initial_field(&ctx->inst[k], h + k * n);
+            if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
+        }
+    }
+    double *dpsi = nullptr;
+    XPFC_CUDA(ctx, cudaMallocAsync((void **)&dpsi, sizeof(double) * n * nb, ctx->stream));
+    cudaError_t e = cudaMemcpyAsync(dpsi, h, sizeof(double) * n * nb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
+    } else {
+        rc = fail(ctx, XPFC_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    }
+    cudaFreeAsync(dpsi, ctx->stream);
+    if (rc != XPFC_OK) return rc;
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->iteration = 0;
+    ctx->initialized = true;
+    ctx->diag_pending = false;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_batch_initialize(xpfc_batch *b, const double *const *fields) {
+    if (!b) return bfail(nullptr, XPFC_EINVAL, "null batch");
+    for (size_t g = 0; g < b->groups.size(); g++) {
+        xpfc_ctx *ctx = b->groups[g];
+        std::vector<const double *> f(ctx->nb, nullptr);
+        if (fields)
+            for (size_t i = 0; i < b->where.size(); i++)
+                if (b->where[i].first == (int)g) f[b->where[i].second] = fields[i];
+        const int rc = init_group(ctx, f);
+        if (rc != XPFC_OK) return bfail(b, rc, "group " + std::to_string(g) + ": " + ctx->err);
+    }
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_batch_step_async(xpfc_batch *b, long long nsteps) {
+    if (!b) return bfail(nullptr, XPFC_EINVAL, "null batch");
+    if (nsteps < 0) return bfail(b, XPFC_EINVAL, "nsteps < 0");
+    for (xpfc_ctx *ctx : b->groups)
+        if (!ctx->initialized) return bfail(b, XPFC_ESTATE, "xpfc_batch_step before xpfc_batch_initialize");
+    // the groups' iterations go out in rounds of kChunk, so that every
+    // group's stream holds work while the host enqueues (a stream's queue of
+    // pending launches is finite: filling one group's first would hold the
+    // host there until that group has nearly finished)
+    constexpr long long kChunk = 16;
+    const size_t ng = b->groups.size();
+    for (size_t g = 0; g < ng; g++) {
+        xpfc_ctx *ctx = b->groups[g];
+        XPFC_CUDA(b, cudaSetDevice(ctx->p.device));
+        const int rc = enqueue_begin(ctx, nsteps, true);
+        if (rc != XPFC_OK) return bfail(b, rc, "group " + std::to_string(g) + ": " + ctx->err);
+    }
+    for (long long c = 0; c < nsteps; c += kChunk) {
+        for (size_t g = 0; g < ng; g++) {
+            xpfc_ctx *ctx = b->groups[g];
+            const long long i0 = ctx->diag_it0 + c, i1 = std::min(ctx->diag_it0 + c + kChunk, ctx->diag_fin);
+            XPFC_CUDA(b, cudaSetDevice(ctx->p.device));
+            const int rc = ctx->esz == 4 ? enqueue_steps<float>(ctx, i0, i1) : enqueue_steps<double>(ctx, i0, i1);
+            if (rc != XPFC_OK) return bfail(b, rc, "group " + std::to_string(g) + ": " + ctx->err);
+        }
+    }
+    for (size_t g = 0; g < ng; g++) {
+        xpfc_ctx *ctx = b->groups[g];
+        XPFC_CUDA(b, cudaSetDevice(ctx->p.device));
+        const int rc = ctx->esz == 4 ? enqueue_end<float>(ctx) : enqueue_end<double>(ctx);
+        if (rc != XPFC_OK) return bfail(b, rc, "group " + std::to_string(g) + ": " + ctx->err);
+    }
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_batch_step(xpfc_batch *b, long long nsteps) {
+    const int rc = xpfc_batch_step_async(b, nsteps);
+    if (rc != XPFC_OK) return rc;
+    for (xpfc_ctx *ctx : b->groups) XPFC_CUDA(b, cudaStreamSynchronize(ctx->stream));
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_batch_collect(xpfc_batch *b, int i, xpfc_diag *out, int cap, int *count) {
+    if (!b) return bfail(nullptr, XPFC_EINVAL, "null batch");
+    if (i < 0 || i >= (int)b->where.size()) return bfail(b, XPFC_EINVAL, "instance index out of range");
+    xpfc_ctx *ctx = b->groups[b->where[i].first];
+    XPFC_CUDA(b, cudaStreamSynchronize(ctx->stream));
+    const int rc = collect_inst(ctx, b->where[i].second, out, cap, count);
+    if (rc != XPFC_OK) b->err = "instance " + std::to_string(i) + ": " + ctx->err;
+    return rc;
+}
+
+extern "C" int xpfc_batch_get_field(xpfc_batch *b, int i, double *host_psi) {
+    if (!b || !host_psi) return bfail(b, XPFC_EINVAL, "null argument");
+    if (i < 0 || i >= (int)b->where.size()) return bfail(b, XPFC_EINVAL, "instance index out of range");
+    xpfc_ctx *ctx = b->groups[b->where[i].first];
+    if (!ctx->initialized) return bfail(b, XPFC_ESTATE, "no field before xpfc_batch_initialize");
+    const int k = b->where[i].second;
+    XPFC_CUDA(b, cudaSetDevice(ctx->p.device));
+    int rc = ctx->esz == 4 ? field_to_X<float>(ctx, k) : field_to_X<double>(ctx, k);
+    if (rc != XPFC_OK) return bfail(b, rc, ctx->err);
+    const size_t n = (size_t)ctx->ncells;
+    rc = host_stage(ctx, ctx->esz * n);
+    if (rc != XPFC_OK) return bfail(b, rc, ctx->err);
+    XPFC_CUDA(b, cudaMemcpyAsync(ctx->hstage, ctx->X, ctx->esz * n, cudaMemcpyDeviceToHost, ctx->stream));
+    XPFC_CUDA(b, cudaStreamSynchronize(ctx->stream));
+    if (ctx->esz == 4) {
+        const float *f = (const float *)ctx->hstage;
+        for (size_t j = 0; j < n; j++) host_psi[j] = (double)f[j];
+    } else {
+        memcpy(host_psi, ctx->hstage, sizeof(double) * n);
+    }
     return XPFC_OK;
 }

@@ -63,6 +63,14 @@ template <typename T> __device__ __forceinline__ T powi(T x, int p, int ref_comp
     return s * s;
 }
 
+// Batched launches: grid z indexes the instance; instance z's field starts
+// z * zstride complex elements after the base pointers and its partial sums
+// follow the other instances' (block_slot).  One field: zstride = 0, nz = 1.
+__device__ __forceinline__ size_t block_slot() {
+    return ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+__host__ __device__ inline unsigned grid_z(int nz) { return nz > 1 ? (unsigned)nz : 1u; }
+
 struct RowArgs {
     const void *in;
     void *out;
@@ -70,9 +78,11 @@ struct RowArgs {
     long long nrows;
     double a, b;
     double scale;         // multiplies the inverse-transform output
-    double *partials;     // [gridDim.x][NQ_ROW] when want_red
+    double *partials;     // [instance][gridDim.x][NQ_ROW] when want_red
     int want_red;
     int ref_compat;
+    long long zstride;    // complex elements between batched instances
+    int nz;               // batched instances (0 or 1: one field)
 };
 
 enum { ROW_FWD = 0, ROW_INV = 1, ROW_FUSED = 2, ROW_NL_FWD = 3 };
@@ -153,7 +163,8 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
     }
     const long long row0 = (long long)blockIdx.x * S::ROWS;
     const int nvalid = (int)min((long long)S::ROWS, args.nrows - row0);
-    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + row0 * L;
+    const long long zoff = (long long)blockIdx.z * args.zstride;
+    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + zoff + row0 * L;
     for (int e = tid; e < nvalid * L; e += S::THREADS) {
         const int r = e / L, c = e - r * L;
         lines[r * SPAN + I::at(c)] = gin[e];
@@ -179,7 +190,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
         const T sc = (T)args.scale;
         const T a = (T)args.a, b = (T)args.b;
         const bool valid = r < nvalid;
-        T *rout = args.real_out ? reinterpret_cast<T *>(args.real_out) + (row0 + r) * (2 * L) : nullptr;
+        T *rout = args.real_out ? reinterpret_cast<T *>(args.real_out) + 2 * zoff + (row0 + r) * (2 * L) : nullptr;
         for (int m = t; m < L; m += S::TPL) {
             cplx<T> z = line[I::at(m)];
             T x0 = z.x, x1 = z.y;
@@ -195,7 +206,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
             }
             line[I::at(m)] = mk<T>(-a * p20 + b * p30, -a * p21 + b * p31);
         }
-        if (args.want_red) block_reduce_store<NQ_ROW>(v, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
+        if (args.want_red) block_reduce_store<NQ_ROW>(v, args.partials + block_slot() * NQ_ROW, sred);
         __syncthreads();
     }
 
@@ -205,7 +216,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
         __syncthreads();
     }
 
-    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + row0 * L;
+    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + zoff + row0 * L;
     for (int e = tid; e < nvalid * L; e += S::THREADS) {
         const int rr = e / L, c = e - rr * L;
         gout[e] = lines[rr * SPAN + I::at(c)];
@@ -229,6 +240,8 @@ struct ColArgs {
     long long ostride;    // stride per blockIdx.y
     double scale;
     int ncols;            // columns in a row (n0/2); the last tile may be partial
+    long long zstride;    // complex elements between batched instances
+    int nz;               // batched instances (0 or 1: one field)
 };
 
 template <typename T, int L, int DIR>
@@ -241,7 +254,8 @@ col_kernel(ColArgs args, const cplx<T> *__restrict__ twL) {
     cplx<T> *tile = stw + L;
     const int tid = threadIdx.x;
     for (int i = tid; i < L; i += S::THREADS) stw[i] = twL[i];
-    const long long base = (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride;
+    const long long base =
+        (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride + (long long)blockIdx.z * args.zstride;
     const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + base;
     const int c = tid % TX, t = tid / TX;
     const bool cvalid = (int)blockIdx.x * TX + c < args.ncols;
@@ -270,6 +284,7 @@ struct KSpace {
     int n0, n1, n2;                 // grid (n0 real axis)
     double dk0sq, dk1sq, dk2sq;     // (2 pi/L_d)^2
     const void *table;              // per shell m: {A, B, c2, k2} in T, or null
+    long long tstride;              // table entries between batched instances
     int mmax;
     // on-the-fly coefficients (no table)
     double dt, Mo, Mo_res, eps;
@@ -279,6 +294,7 @@ struct KSpace {
     int noise_on;
     double noise_scale;             // amp * sqrt(cells)
     unsigned long long noise_seed;
+    const unsigned long long *seeds; // per batched instance (null: noise_seed)
     long long step;
     // the same constants in FP32 for the mixed path (no FP64 work per mode)
     float f_dk0sq, f_dk1sq, f_dk2sq, f_dt, f_Mo, f_eps, f_noise_scale;
@@ -294,7 +310,7 @@ __device__ __forceinline__ Coef<T> kcoef(const KSpace &ks, int i0, int i1, int i
     const int s1 = signed_idx(i1, ks.n1), s2 = signed_idx(i2, ks.n2);
     Coef<T> r;
     if (ks.table) {
-        const int m = i0 * i0 + s1 * s1 + s2 * s2;
+        const long long m = (long long)blockIdx.z * ks.tstride + (i0 * i0 + s1 * s1 + s2 * s2);
         if constexpr (sizeof(T) == 4) {
             const float4 e = __ldg(reinterpret_cast<const float4 *>(ks.table) + m);
             r.A = e.x; r.B = e.y; r.c2 = e.z; r.k2 = e.w;
@@ -361,9 +377,10 @@ __device__ __forceinline__ uint4 noise_draw(const KSpace &ks, int c0, int c1, in
         ctr = (long long)(c1 % (ks.n1 / 2)) * ks.n0 + c0;
     }
     const unsigned long long stream = 1ull + (unsigned long long)ks.step;
+    const unsigned long long seed = ks.seeds ? ks.seeds[blockIdx.z] : ks.noise_seed;
     return philox4x32_10<ROLLED>(make_uint4((uint32_t)ctr, (uint32_t)((unsigned long long)ctr >> 32), (uint32_t)stream,
                                             (uint32_t)(stream >> 32)),
-                                 make_uint2((uint32_t)ks.noise_seed, (uint32_t)(ks.noise_seed >> 32)));
+                                 make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
 }
 
 template <typename T> __device__ __forceinline__ T noise_amp_of(const KSpace &ks, T k2) {
@@ -425,7 +442,13 @@ struct PenArgs {
     double *partials;
     int pin;             // overwrite the k = 0 mode with pin_value (unscaled)
     double pin_value;
+    const double *pin_values;   // per batched instance (null: pin_value)
+    long long zstride;   // complex elements between batched instances
+    int nz;              // batched instances (0 or 1: one field)
 };
+__device__ __forceinline__ double pin_of(const PenArgs &a) {
+    return a.pin_values ? a.pin_values[blockIdx.z] : a.pin_value;
+}
 
 template <typename T, int L, int NG>
 __global__ void __launch_bounds__(PenShape<T, L, NG>::THREADS)
@@ -448,8 +471,8 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
     yg[1] = (NG == 2) ? (ks.n1 - p) % ks.n1 : p;
     const int G = (NG == 2 && yg[1] != yg[0]) ? 2 : 1;
     const int kx0 = blockIdx.x * TX;
-    cplx<T> *gS = reinterpret_cast<cplx<T> *>(args.S);
-    const cplx<T> *gW = reinterpret_cast<const cplx<T> *>(args.W);
+    cplx<T> *gS = reinterpret_cast<cplx<T> *>(args.S) + (long long)blockIdx.z * args.zstride;
+    const cplx<T> *gW = reinterpret_cast<const cplx<T> *>(args.W) + (long long)blockIdx.z * args.zstride;
 
     // load
     {
@@ -518,7 +541,7 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
             }
             cplx<T> x0n = mk<T>(c0.A * num0.x + c0.B * w0.x, c0.A * num0.y + c0.B * w0.y);
             cplx<T> xNn = mk<T>(cN.A * numN.x + cN.B * wN.x, cN.A * numN.y + cN.B * wN.y);
-            if (args.pin && i1 == 0 && i2 == 0) x0n = mk<T>((T)args.pin_value, (T)0);
+            if (args.pin && i1 == 0 && i2 == 0) x0n = mk<T>((T)pin_of(args), (T)0);
             if (args.want_red) {
                 const double k20 = c0.k2, c20 = c0.c2, k2N = cN.k2, c2N = cN.c2;
                 v[0] += c20 * ((double)s0.x * s0.x + (double)s0.y * s0.y);
@@ -536,7 +559,7 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
         res[q] = out;
     }
     if (args.want_red)
-        block_reduce_store<NQ_PEN>(v, args.partials + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * NQ_PEN, sred);
+        block_reduce_store<NQ_PEN>(v, args.partials + block_slot() * NQ_PEN, sred);
     if (!args.update) return;
     __syncthreads();
 #pragma unroll
@@ -573,10 +596,13 @@ template <typename T, int L, int NG> constexpr size_t pen_smem_bytes() {
 // Deterministic final reduction of per-block partials: out[q] = sum_b part[b][q]
 // (one block; fixed order for a fixed partial count).
 // ---------------------------------------------------------------------------
+// Batched: block z reduces instance z's partials into out + z * ostride.
 template <int NQ>
 __global__ void __launch_bounds__(256) finalize_kernel(const double *__restrict__ part, long long nparts,
-                                                       double *__restrict__ out) {
+                                                       double *__restrict__ out, long long ostride) {
     __shared__ double sred[32 * NQ];
+    part += (size_t)blockIdx.z * nparts * NQ;
+    out += (size_t)blockIdx.z * ostride;
     double v[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; q++) v[q] = 0.0;

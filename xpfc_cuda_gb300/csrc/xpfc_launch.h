@@ -35,7 +35,9 @@ cudaError_t launch_density(const T *psi, const T *p2, const T *p3, const T *p4, 
                            double b, int square, int ref_compat, double *partials, cudaStream_t s, int *nblocks);
 cudaError_t launch_convert_d2f(const double *in, float *out, long long n, cudaStream_t s);
 cudaError_t launch_convert_f2d(const float *in, double *out, long long n, cudaStream_t s);
-cudaError_t launch_finalize(int nq, const double *part, long long nparts, double *out, cudaStream_t s);
+// ninst instances: instance z reduces part[z * nparts * nq ...] into out + z * ostride
+cudaError_t launch_finalize(int nq, const double *part, long long nparts, double *out, cudaStream_t s, int ninst = 1,
+                            long long ostride = 0);
 
 // grid shapes the launchers use (for sizing the partials buffer)
 int row_rows(int L);

@@ -65,7 +65,8 @@ col_kernel_reg(ColArgs args, const cplx<T> *__restrict__ twN) {
     for (int i = tid; i < N; i += S::THREADS) stw[i] = twN[i];
     const int c = tid % TX, t = tid / TX;
     const bool cvalid = (int)blockIdx.x * TX + c < args.ncols;
-    const long long base = (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride + c;
+    const long long base = (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride +
+                           (long long)blockIdx.z * args.zstride + c;
     const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + base;
     cplx<T> v[P];
 #pragma unroll
@@ -163,7 +164,8 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
     const int r = tid / Q, t = tid % Q, lane = tid & 31;
     const long long row = (long long)blockIdx.x * S::ROWS + r;
     const bool valid = row < args.nrows;
-    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + row * N + t;
+    const long long zoff = (long long)blockIdx.z * args.zstride;
+    const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + zoff + row * N + t;
     cplx<T> v[P];
 #pragma unroll
     for (int j = 0; j < P; j++) v[j] = valid ? gin[Q * j] : mk<T>((T)0, (T)0);
@@ -182,7 +184,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
         DSum<T, NQ_ROW> acc;
         const T sc = (T)args.scale;
         const T a = (T)args.a, b = (T)args.b;
-        T *rout = args.real_out ? reinterpret_cast<T *>(args.real_out) + row * (2 * N) : nullptr;
+        T *rout = args.real_out ? reinterpret_cast<T *>(args.real_out) + 2 * zoff + row * (2 * N) : nullptr;
 #pragma unroll
         for (int j = 0; j < P; j++) {
             T x0 = v[j].x, x1 = v[j].y;
@@ -207,7 +209,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
             double tot[NQ_ROW];
 #pragma unroll
             for (int q = 0; q < NQ_ROW; q++) tot[q] = acc.get(q);
-            block_reduce_store<NQ_ROW>(tot, args.partials + (size_t)blockIdx.x * NQ_ROW, sred);
+            block_reduce_store<NQ_ROW>(tot, args.partials + block_slot() * NQ_ROW, sred);
         }
     }
     if (MODE != ROW_INV) {
@@ -215,7 +217,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
         reg_pack<T, N>(v, t, lane, stw2);
     }
     if (!valid) return;
-    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + row * N + t;
+    cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + zoff + row * N + t;
 #pragma unroll
     for (int j = 0; j < P; j++) gout[Q * j] = v[j];
 }
@@ -281,7 +283,7 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const PenArgs &
     if (ks.noise_on) noise = noise_at<T>(ks, i0, i1, i2, cf.k2);
     const cplx<T> num = cadd(xs, noise);
     cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
-    if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)args.pin_value, (T)0);
+    if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)pin_of(args), (T)0);
     if (args.want_red) diag_mode<T>(ks, cf, xs, xw, noise, xn, acc, weight);
     return xn;
 }
@@ -306,7 +308,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     const int yg = (g == 0) ? y1 : y2;
     const int kx0 = blockIdx.x * TX;
     const bool valid = (g < G) && (kx0 + c < args.L0);
-    const long long off = (long long)yg * args.gstride + kx0 + c;
+    const long long off = (long long)blockIdx.z * args.zstride + (long long)yg * args.gstride + kx0 + c;
     cplx<T> *gS = reinterpret_cast<cplx<T> *>(args.S) + off;
     const cplx<T> *gW = reinterpret_cast<const cplx<T> *>(args.W) + off;
     cplx<T> vs[P], vw[P];
@@ -381,7 +383,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     }
     if (RED) {
         double tot[NQ_PEN] = {acc.get(0), acc.get(1)};
-        block_reduce_store<NQ_PEN>(tot, args.partials + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * NQ_PEN, sred);
+        block_reduce_store<NQ_PEN>(tot, args.partials + block_slot() * NQ_PEN, sred);
     }
     if (!args.update) return;
     reg_fft<T, N, +1>(vs, t, bufS + ln * S::LP, stw);
