@@ -63,6 +63,17 @@ template <typename T> __device__ __forceinline__ T powi(T x, int p, int ref_comp
     return s * s;
 }
 
+// Programmatic dependent launch.  The step's passes are launched with
+// programmatic stream serialisation, so a pass's blocks may be scheduled while
+// the previous pass drains; each pass reads only constant tables (twiddles)
+// before pdl_wait(), which blocks until the previous grid has completed and
+// its writes are visible, and then lets the next pass start launching.
+// Without the launch attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Batched launches: grid z indexes the instance; instance z's field starts
 // z * zstride complex elements after the base pointers and its partial sums
 // follow the other instances' (block_slot).  One field: zstride = 0, nz = 1.
@@ -161,6 +172,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
         stw[i] = twL[i];
         stw2[i] = tw2L[i];
     }
+    pdl_wait();
     const long long row0 = (long long)blockIdx.x * S::ROWS;
     const int nvalid = (int)min((long long)S::ROWS, args.nrows - row0);
     const long long zoff = (long long)blockIdx.z * args.zstride;
@@ -254,6 +266,7 @@ col_kernel(ColArgs args, const cplx<T> *__restrict__ twL) {
     cplx<T> *tile = stw + L;
     const int tid = threadIdx.x;
     for (int i = tid; i < L; i += S::THREADS) stw[i] = twL[i];
+    pdl_wait();
     const long long base =
         (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride + (long long)blockIdx.z * args.zstride;
     const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + base;
@@ -464,6 +477,7 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
 
     const int tid = threadIdx.x;
     for (int i = tid; i < L; i += S::THREADS) stw[i] = twL[i];
+    pdl_wait();
 
     const int p = blockIdx.y;
     int yg[2];
@@ -601,6 +615,7 @@ template <int NQ>
 __global__ void __launch_bounds__(256) finalize_kernel(const double *__restrict__ part, long long nparts,
                                                        double *__restrict__ out, long long ostride) {
     __shared__ double sred[32 * NQ];
+    pdl_wait();
     part += (size_t)blockIdx.z * nparts * NQ;
     out += (size_t)blockIdx.z * ostride;
     double v[NQ];

@@ -63,6 +63,7 @@ col_kernel_reg(ColArgs args, const cplx<T> *__restrict__ twN) {
     cplx<T> *buf = stw + N;
     const int tid = threadIdx.x;
     for (int i = tid; i < N; i += S::THREADS) stw[i] = twN[i];
+    pdl_wait();
     const int c = tid % TX, t = tid / TX;
     const bool cvalid = (int)blockIdx.x * TX + c < args.ncols;
     const long long base = (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride +
@@ -161,6 +162,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
         stw[i] = twN[i];
         stw2[i] = tw2N[i];
     }
+    pdl_wait();
     const int r = tid / Q, t = tid % Q, lane = tid & 31;
     const long long row = (long long)blockIdx.x * S::ROWS + r;
     const bool valid = row < args.nrows;
@@ -300,6 +302,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     double *sred = reinterpret_cast<double *>(bufW + S::LINES * S::LP);
     const int tid = threadIdx.x;
     for (int i = tid; i < N; i += S::THREADS) stw[i] = twN[i];
+    pdl_wait();
 
     const int c = tid % TX, t = (tid / TX) % Q, g = tid / (TX * Q);
     const int p = blockIdx.y;
