@@ -134,12 +134,20 @@ int xpfc_get_params(const xpfc_ctx *ctx, xpfc_params *p);
 /* Host pointer to the stream the context launches on (cudaStream_t). */
 void *xpfc_get_stream(const xpfc_ctx *ctx);
 
-/* initialize.cu:6-238 + main.cu:226: builds (host_psi == NULL) or takes the
-   initial field, pins its mean to psi0 (Avg_calc.cu:21-43), uploads it and
-   prepares both the staged buffers (XPFC_BUF_PSI) and the fused state. */
+/* initialize.cu:6-238 + main.cu:226: builds (host_psi == NULL: on the device,
+   except the VTK restart, read on the host) or takes the initial field, pins
+   its mean to psi0 (Avg_calc.cu:21-43), uploads it and prepares both the
+   staged buffers (XPFC_BUF_PSI) and the fused state. */
 int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi);
-/* Host-side initial field exactly as xpfc_initialize would build it. */
+/* The initial field of p on the host (every generator, mean pinned). */
 int xpfc_build_initial_field(const xpfc_params *p, double *host_psi);
+/* The same on the device: dev_psi holds Mx*My*Mz doubles; stream is a
+   cudaStream_t (NULL: the legacy default stream); returns when the field is
+   ready.  Every generator but the VTK restart (iconfig 10, a host file).
+   No reference counterpart (the reference builds fields on the host,
+   initialize.cu:95-197); agrees with xpfc_build_initial_field to rounding
+   (device and host libm differ in the last bits). */
+int xpfc_build_initial_field_device(const xpfc_params *p, double *dev_psi, void *stream);
 
 /* ---- fused step: the hot path ------------------------------------------ */
 /* Advances nsteps iterations of main.cu:306-435 with the fused passes.
@@ -228,6 +236,55 @@ int xpfc_batch_step_async(xpfc_batch *b, long long nsteps);
    (XPFC_ENONFINITE when its F or mean is not finite). */
 int xpfc_batch_collect(xpfc_batch *b, int i, xpfc_diag *out, int cap, int *count);
 int xpfc_batch_get_field(xpfc_batch *b, int i, double *host_psi);
+
+/* ---- serving ------------------------------------------------------------------ */
+/* No counterpart in the reference, which runs one solve per process.  A server
+   runs solve requests on one GPU from a scheduler thread of its own: queued
+   requests are admitted in arrival order while their device memory fits
+   hbm_budget_bytes and fewer than max_running solves are in flight; each
+   running solve has a context with its own stream (reused across requests of
+   the same grid and precision) and its iterations are enqueued chunk_steps at
+   a time, round robin, so solves join and leave the running set at chunk
+   boundaries while the GPU interleaves them.  A request's diagnostics and
+   field are those xpfc_step gives for the same params alone.  Initial fields
+   come from the params' generator on the device, or from the caller. */
+typedef struct xpfc_server xpfc_server;
+typedef struct {
+    size_t hbm_budget_bytes;  /* device memory for solves (0: 80% of free memory) */
+    int max_running;          /* solves in flight (0: 16)                        */
+    int chunk_steps;          /* iterations per solve per round (0: 16)          */
+    int device;
+} xpfc_server_config;
+typedef enum { XPFC_REQ_QUEUED = 0, XPFC_REQ_RUNNING = 1, XPFC_REQ_DONE = 2, XPFC_REQ_FAILED = 3 } xpfc_req_state;
+typedef struct {
+    long long id;
+    int state;                          /* xpfc_req_state                      */
+    int status;                         /* xpfc_status of a finished request   */
+    double t_submit, t_admit, t_done;   /* seconds since the server started    */
+    size_t device_bytes;                /* device memory held while it runs    */
+} xpfc_request_info;
+typedef struct {
+    long long submitted, queued, running, done, failed;
+    long long contexts_created, contexts_reused;
+    size_t bytes_in_use, peak_bytes_in_use, budget;
+} xpfc_server_stats;
+int xpfc_server_create(const xpfc_server_config *cfg, xpfc_server **out);
+/* Running solves finish; queued ones fail (XPFC_ESTATE). */
+int xpfc_server_destroy(xpfc_server *s);
+const char *xpfc_server_last_error(const xpfc_server *s);
+/* host_psi: NULL (the params' generator) or a field the call copies;
+   keep_field = 1 keeps the final field for xpfc_server_result. */
+int xpfc_server_submit(xpfc_server *s, const xpfc_params *p, const double *host_psi, long long nsteps,
+                       int keep_field, long long *id);
+/* Blocks until the request finished (timeout_s < 0: no limit; XPFC_ETIMEDOUT). */
+int xpfc_server_wait(xpfc_server *s, long long id, double timeout_s);
+int xpfc_server_info(xpfc_server *s, long long id, xpfc_request_info *info);
+/* Final field (when kept; host_psi may be NULL) and diagnostics of a
+   finished request; a failed request returns its status. */
+int xpfc_server_result(xpfc_server *s, long long id, double *host_psi, xpfc_diag *out, int cap, int *count);
+/* Forgets a finished request. */
+int xpfc_server_release(xpfc_server *s, long long id);
+int xpfc_server_stats_get(xpfc_server *s, xpfc_server_stats *st);
 
 /* ---- allocation-free reduction ---------------------------------------------- */
 /* No counterpart in the reference.  The free energy of xpfc_FE_calc

@@ -46,6 +46,13 @@ def test_params_layout_matches_header(tmp_path):
     fields = ["Mx", "Lx", "psi0", "nsteps", "t_sample", "npeaks", "pk_k", "pk_beta", "envelope", "ff_factor",
               "noise_seed", "ic_kind", "A_10", "roa", "ic_seed", "ic_seed_radius", "vtk_path", "device", "stream"]
     body = "".join('printf("%%s %%zu\\n", "%s", offsetof(xpfc_params, %s));\n' % (f, f) for f in fields)
+    from xpfc_cuda_gb300 import _lib as LB
+    server_body = ""
+    for struct, cls in (("xpfc_server_config", LB.XpfcServerConfig), ("xpfc_request_info", LB.XpfcRequestInfo),
+                        ("xpfc_server_stats", LB.XpfcServerStats)):
+        server_body += 'printf("%s %%zu\\n", sizeof(%s));\n' % (struct, struct)
+        server_body += "".join('printf("%s.%s %%zu\\n", offsetof(%s, %s));\n' % (struct, f, struct, f)
+                               for f, _ in cls._fields_)
     prog.write_text(textwrap.dedent("""
         #include <stdio.h>
         #include <stddef.h>
@@ -53,13 +60,19 @@ def test_params_layout_matches_header(tmp_path):
         int main(void) {
         printf("sizeof %zu\\n", sizeof(xpfc_params));
         printf("diag %zu\\n", sizeof(xpfc_diag));
-        """) + body + "return 0; }\n")
+        """) + body + server_body + "return 0; }\n")
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(prog), "-o", str(exe)], check=True)
     out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split("\n")
                if line)
     assert int(out["sizeof"]) == C.sizeof(XpfcParams)
     assert int(out["diag"]) == C.sizeof(XpfcDiag)
+    from xpfc_cuda_gb300 import _lib
+    for struct, cls in (("xpfc_server_config", _lib.XpfcServerConfig), ("xpfc_request_info", _lib.XpfcRequestInfo),
+                        ("xpfc_server_stats", _lib.XpfcServerStats)):
+        assert int(out[struct]) == C.sizeof(cls), struct
+        for f, _ in cls._fields_:
+            assert int(out[struct + "." + f]) == getattr(cls, f).offset, (struct, f)
     for f in fields:
         assert int(out[f]) == getattr(XpfcParams, f).offset, f
 

@@ -53,6 +53,26 @@ class XpfcDiag(C.Structure):
                 ("has", C.c_int)]
 
 
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
+
+
+class XpfcServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_running", C.c_int), ("chunk_steps", C.c_int),
+                ("device", C.c_int)]
+
+
+class XpfcRequestInfo(C.Structure):
+    _fields_ = [("id", C.c_longlong), ("state", C.c_int), ("status", C.c_int), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("device_bytes", C.c_size_t)]
+
+
+class XpfcServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("queued", C.c_longlong), ("running", C.c_longlong),
+                ("done", C.c_longlong), ("failed", C.c_longlong), ("contexts_created", C.c_longlong),
+                ("contexts_reused", C.c_longlong), ("bytes_in_use", C.c_size_t),
+                ("peak_bytes_in_use", C.c_size_t), ("budget", C.c_size_t)]
+
+
 # (name, restype, argtypes) for every entry point of include/xpfc.h
 _dp = C.POINTER(C.c_double)
 _ctx = C.c_void_p
@@ -66,6 +86,7 @@ SIGNATURES = [
     ("xpfc_get_stream", C.c_void_p, [_ctx]),
     ("xpfc_initialize", C.c_int, [_ctx, _dp]),
     ("xpfc_build_initial_field", C.c_int, [C.POINTER(XpfcParams), _dp]),
+    ("xpfc_build_initial_field_device", C.c_int, [C.POINTER(XpfcParams), C.c_void_p, C.c_void_p]),
     ("xpfc_step", C.c_int, [_ctx, C.c_longlong, C.POINTER(XpfcDiag), C.c_int, C.POINTER(C.c_int)]),
     ("xpfc_step_async", C.c_int, [_ctx, C.c_longlong]),
     ("xpfc_collect", C.c_int, [_ctx, C.POINTER(XpfcDiag), C.c_int, C.POINTER(C.c_int)]),
@@ -101,6 +122,17 @@ SIGNATURES = [
     ("xpfc_batch_step_async", C.c_int, [C.c_void_p, C.c_longlong]),
     ("xpfc_batch_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(XpfcDiag), C.c_int, C.POINTER(C.c_int)]),
     ("xpfc_batch_get_field", C.c_int, [C.c_void_p, C.c_int, _dp]),
+    ("xpfc_server_create", C.c_int, [C.POINTER(XpfcServerConfig), C.POINTER(C.c_void_p)]),
+    ("xpfc_server_destroy", C.c_int, [C.c_void_p]),
+    ("xpfc_server_last_error", C.c_char_p, [C.c_void_p]),
+    ("xpfc_server_submit", C.c_int, [C.c_void_p, C.POINTER(XpfcParams), _dp, C.c_longlong, C.c_int,
+                                     C.POINTER(C.c_longlong)]),
+    ("xpfc_server_wait", C.c_int, [C.c_void_p, C.c_longlong, C.c_double]),
+    ("xpfc_server_info", C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(XpfcRequestInfo)]),
+    ("xpfc_server_result", C.c_int, [C.c_void_p, C.c_longlong, _dp, C.POINTER(XpfcDiag), C.c_int,
+                                     C.POINTER(C.c_int)]),
+    ("xpfc_server_release", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("xpfc_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(XpfcServerStats)]),
     ("xpfc_FE_calc_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong,
                                         C.c_double, C.c_double, C.c_double, _dp, C.c_void_p]),
     ("xpfc_launch_count", C.c_longlong, [_ctx]),

@@ -71,6 +71,11 @@ def build_initial_field(p):
     return out
 
 
+def build_initial_field_device(p, dev_ptr, stream=None):
+    """The same field built on the device into dev_ptr (Mx*My*Mz doubles)."""
+    _check(_lib.load().xpfc_build_initial_field_device(C.byref(p), C.c_void_p(dev_ptr), C.c_void_p(stream or 0)))
+
+
 def writeVTKFile(path, psi, Mx, My, Mz=1, Lx=1.0, Ly=1.0, Lz=1.0, precision=6):
     """write_vtk.cu:4-35 (x fastest in the file, `precision` significant digits)."""
     psi = np.ascontiguousarray(psi, dtype=np.float64)
@@ -340,6 +345,89 @@ class Batch:
         out = np.empty(p.Mx * p.My * p.Mz)
         self._c(self._L.xpfc_batch_get_field(self._h, i, _dp(out)))
         return out.reshape(p.Mx, p.My, p.Mz)
+
+
+class Server:
+    """Solve requests on one GPU (an xpfc_server): admission under a device
+    memory budget, up to max_running solves interleaved on their own streams."""
+
+    def __init__(self, hbm_budget_bytes=0, max_running=16, chunk_steps=16, device=0):
+        self._L = _lib.load()
+        cfg = _lib.XpfcServerConfig(hbm_budget_bytes, max_running, chunk_steps, device)
+        h = C.c_void_p()
+        rc = self._L.xpfc_server_create(C.byref(cfg), C.byref(h))
+        if rc != _lib.OK:
+            msg = self._L.xpfc_server_last_error(None)
+            raise XpfcError(rc, msg.decode() if msg else "")
+        self._h = h
+
+    def _c(self, rc):
+        if rc != _lib.OK:
+            msg = self._L.xpfc_server_last_error(self._h)
+            raise XpfcError(rc, msg.decode() if msg else "")
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.xpfc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, params, nsteps, field=None, keep_field=False):
+        """Queue a solve of nsteps iterations; returns its request id."""
+        rid = C.c_longlong()
+        if field is None:
+            self._c(self._L.xpfc_server_submit(self._h, C.byref(params), None, nsteps, int(keep_field),
+                                               C.byref(rid)))
+        else:
+            a = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
+            if a.size != params.Mx * params.My * params.Mz:
+                raise ValueError("field size does not match the grid")
+            self._c(self._L.xpfc_server_submit(self._h, C.byref(params), _dp(a), nsteps, int(keep_field),
+                                               C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid, timeout=-1.0):
+        self._c(self._L.xpfc_server_wait(self._h, rid, timeout))
+
+    def info(self, rid):
+        i = _lib.XpfcRequestInfo()
+        self._c(self._L.xpfc_server_info(self._h, rid, C.byref(i)))
+        return {"id": i.id, "state": i.state, "status": i.status, "t_submit": i.t_submit, "t_admit": i.t_admit,
+                "t_done": i.t_done, "device_bytes": i.device_bytes}
+
+    def result(self, rid, shape=None, cap=256):
+        """(field or None, diagnostics) of a finished request; shape = the
+        request's (Mx, My, Mz) when its field was kept."""
+        recs = (XpfcDiag * cap)()
+        cnt = C.c_int(0)
+        out = None
+        if shape is not None:
+            out = np.empty(shape[0] * shape[1] * shape[2])
+            self._c(self._L.xpfc_server_result(self._h, rid, _dp(out), recs, cap, C.byref(cnt)))
+            out = out.reshape(shape)
+        else:
+            self._c(self._L.xpfc_server_result(self._h, rid, None, recs, cap, C.byref(cnt)))
+        return out, _records(recs, cnt.value)
+
+    def release(self, rid):
+        self._c(self._L.xpfc_server_release(self._h, rid))
+
+    def stats(self):
+        st = _lib.XpfcServerStats()
+        self._c(self._L.xpfc_server_stats_get(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
 
 
 def run_reference_loop(x, nsteps, t_sample):

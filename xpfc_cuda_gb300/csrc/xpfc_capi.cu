@@ -284,7 +284,13 @@ static int build_tables(xpfc_ctx *ctx) {
     // one coefficient set per shell m = i0^2 + i1^2 + i2^2 when the k-grid
     // spacing is the same on every axis (equal box lengths)
     const bool cubic = (ctx->Lax[0] == ctx->Lax[1]) && (ctx->n2 == 1 || ctx->Lax[0] == ctx->Lax[2]);
-    if (!cubic) return XPFC_OK;
+    if (!cubic) {
+        // coefficients on the fly; a reused context drops the tables of its last params
+        cudaFree(ctx->table_d);
+        cudaFree(ctx->table_f);
+        ctx->table_d = ctx->table_f = nullptr;
+        return XPFC_OK;
+    }
     const int h0 = ctx->n0 / 2, h1 = ctx->n1 / 2, h2 = ctx->n2 / 2;
     ctx->mmax = h0 * h0 + h1 * h1 + h2 * h2;
     const size_t nm = (size_t)ctx->mmax + 1;
@@ -305,10 +311,14 @@ static int build_tables(xpfc_ctx *ctx) {
         }
     }
     for (size_t j = 0; j < td.size(); j++) tf[j] = (float)td[j];
-    XPFC_CUDA(ctx, cudaMalloc(&ctx->table_d, sizeof(double) * td.size()));
-    XPFC_CUDA(ctx, cudaMalloc(&ctx->table_f, sizeof(float) * tf.size()));
-    XPFC_CUDA(ctx, cudaMemcpy(ctx->table_d, td.data(), sizeof(double) * td.size(), cudaMemcpyHostToDevice));
-    XPFC_CUDA(ctx, cudaMemcpy(ctx->table_f, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice));
+    // the size depends only on the grid and nb, so a reused context keeps its buffers
+    if (!ctx->table_d) XPFC_CUDA(ctx, cudaMalloc(&ctx->table_d, sizeof(double) * td.size()));
+    if (!ctx->table_f) XPFC_CUDA(ctx, cudaMalloc(&ctx->table_f, sizeof(float) * tf.size()));
+    // pageable sources: each call returns once its source is staged
+    XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->table_d, td.data(), sizeof(double) * td.size(), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->table_f, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice,
+                                   ctx->stream));
     return XPFC_OK;
 }
 
@@ -397,7 +407,7 @@ static int create_group(const xpfc_params *ps, int nb, xpfc_ctx **out) {
                                      : (ctx->three_d ? pen_tx<double>(ctx->n2, 2) : pen_tx<double>(ctx->n1, 1));
         const size_t penblk = (size_t)(L0 / tx + 1) * (ctx->n1 / 2 + 1);
         ctx->part_per_inst = std::max(rowblk * NQ_ROW, penblk * NQ_PEN);
-        const size_t need = std::max(ctx->part_per_inst * nb, (size_t)DENSITY_BLOCKS);
+        const size_t need = std::max(ctx->part_per_inst * nb, (size_t)IC_SCRATCH);
         rc = ensure_partials(ctx, need);
     }
     if (rc == XPFC_OK && cudaMalloc(&ctx->init_red, sizeof(double) * 8 * nb) != cudaSuccess) rc = XPFC_ENOMEM;
@@ -578,23 +588,110 @@ static int init_fused(xpfc_ctx *ctx, const double *dpsi) {
     return XPFC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// initial fields on the device (every generator but the VTK restart)
+// ---------------------------------------------------------------------------
+static bool ic_on_device(const xpfc_params &p) { return !(p.ic_kind == XPFC_IC_REFERENCE && p.iconfig == 10); }
+
+// Enqueues p's initial field (mean pinned to psi0) into dpsi on stream s;
+// scratch: IC_SCRATCH device doubles.  Returns a status and sets *why.
+static int enqueue_initial_field(const xpfc_params &p, double *dpsi, double *scratch, cudaStream_t s,
+                                 std::string *why) {
+    ICArgs a{};
+    a.Mx = p.Mx; a.My = p.My; a.Mz = p.Mz;
+    a.Lx = p.Lx; a.Ly = p.Ly; a.Lz = p.Lz;
+    a.psi0 = p.psi0;
+    a.amp = p.ic_amp;
+    a.seed = p.ic_seed;
+    a.seed_amp = p.ic_seed_amp;
+    a.seed_radius = p.ic_seed_radius;
+    a.iconfig = p.iconfig; a.iseed = p.iseed; a.ishape = p.ishape;
+    a.A_10 = p.A_10; a.A_11 = p.A_11; a.A_tri = p.A_tri;
+    a.h = p.h; a.k = p.k; a.roa = p.roa;
+    double *coords = nullptr;
+    switch (p.ic_kind) {
+        case XPFC_IC_NOISE: a.kind = IC_DEV_NOISE; break;
+        case XPFC_IC_FCC_SEED: a.kind = IC_DEV_FCC_SEED; break;
+        case XPFC_IC_REFERENCE: {
+            if (p.iconfig == 10) {
+                *why = "the VTK restart is read on the host";
+                return XPFC_EINVAL;
+            }
+            if (p.Mz != 1) {
+                *why = "reference initial conditions are 2-D (Mz must be 1)";
+                return XPFC_EINVAL;
+            }
+            a.kind = IC_DEV_REFERENCE;
+            // linspace.cu:5-18: accumulated coordinates, du = L/(M-1), summed in order
+            std::vector<double> c((size_t)p.Mx + p.My + 2);
+            const double dux = p.Lx / ((double)p.Mx - 1), duy = p.Ly / ((double)p.My - 1);
+            c[0] = 0.0;
+            for (int i = 0; i < p.Mx; i++) c[i + 1] = c[i] + dux;
+            double *cy = c.data() + p.Mx + 1;
+            cy[0] = 0.0;
+            for (int j = 0; j < p.My; j++) cy[j + 1] = cy[j] + duy;
+            cudaError_t e = cudaMallocAsync((void **)&coords, sizeof(double) * c.size(), s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(coords, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) {
+                *why = std::string("coordinates: ") + cudaGetErrorString(e);
+                return XPFC_ECUDA;
+            }
+            a.xs = coords;
+            a.ys = coords + p.Mx + 1;
+            break;
+        }
+        default: *why = "unknown ic_kind"; return XPFC_EINVAL;
+    }
+    cudaError_t e = launch_initial_field(a, dpsi, scratch, s);
+    if (coords) cudaFreeAsync(coords, s);
+    if (e != cudaSuccess) {
+        *why = std::string("initial field: ") + cudaGetErrorString(e);
+        return XPFC_ECUDA;
+    }
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_build_initial_field_device(const xpfc_params *p, double *dev_psi, void *stream) {
+    if (!p || !dev_psi) return fail(nullptr, XPFC_EINVAL, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    double *scratch = nullptr;
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&scratch, sizeof(double) * IC_SCRATCH, s);
+    if (e != cudaSuccess) return fail(nullptr, XPFC_ECUDA, std::string("scratch: ") + cudaGetErrorString(e));
+    std::string why;
+    const int rc = enqueue_initial_field(*p, dev_psi, scratch, s, &why);
+    cudaFreeAsync(scratch, s);
+    if (rc != XPFC_OK) return fail(nullptr, rc, why);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(nullptr, XPFC_ECUDA, cudaGetErrorString(e));
+    return XPFC_OK;
+}
+
 extern "C" int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi) {
     if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
     XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
     const size_t n = (size_t)ctx->ncells;
-    int rc = host_stage(ctx, sizeof(double) * n);
-    if (rc != XPFC_OK) return rc;
-    double *h = (double *)ctx->hstage;
-    if (host_psi) {
-        memcpy(h, host_psi, sizeof(double) * n);
-        pin_mean(h, n, ctx->p.psi0);          // configure_avg_density, Avg_calc.cu:21-43
-    } else {
-        rc = build_initial_field(&ctx->p, h);
-        if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
-    }
     double *dpsi = staged_buf(ctx, XPFC_BUF_PSI);
     if (!dpsi) return fail(ctx, XPFC_ENOMEM, "staged buffer allocation failed");
-    XPFC_CUDA(ctx, cudaMemcpyAsync(dpsi, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    int rc = XPFC_OK;
+    if (!host_psi && ic_on_device(ctx->p)) {
+        std::string why;
+        rc = enqueue_initial_field(ctx->p, dpsi, ctx->partials, ctx->stream, &why);
+        if (rc != XPFC_OK) return fail(ctx, rc, why);
+    } else {
+        rc = host_stage(ctx, sizeof(double) * n);
+        if (rc != XPFC_OK) return rc;
+        double *h = (double *)ctx->hstage;
+        if (host_psi) {
+            memcpy(h, host_psi, sizeof(double) * n);
+            pin_mean(h, n, ctx->p.psi0);          // configure_avg_density, Avg_calc.cu:21-43
+        } else {
+            rc = build_initial_field(&ctx->p, h);   // the VTK restart
+            if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
+        }
+        XPFC_CUDA(ctx, cudaMemcpyAsync(dpsi, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    }
     rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
     if (rc != XPFC_OK) return rc;
     XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1205,13 +1302,21 @@ extern "C" int xpfc_batch_group_of(const xpfc_batch *b, int i) {
 static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) {
     XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
     const size_t n = (size_t)ctx->ncells, nb = (size_t)ctx->nb;
-    int rc = host_stage(ctx, sizeof(double) * n * nb);
+    int rc = XPFC_OK;
+    bool need_host = false;
+    for (size_t k = 0; k < nb; k++) need_host |= fields[k] != nullptr || !ic_on_device(ctx->inst[k]);
+    if (need_host) rc = host_stage(ctx, sizeof(double) * n * nb);
     if (rc != XPFC_OK) return rc;
     double *h = (double *)ctx->hstage;
+    // host fields (given, or the VTK restart) go up in one copy per run of
+    // consecutive instances; the other generators run on the device
+    std::vector<char> on_dev(nb, 0);
     for (size_t k = 0; k < nb; k++) {
         if (fields[k]) {
             memcpy(h + k * n, fields[k], sizeof(double) * n);
             pin_mean(h + k * n, n, ctx->inst[k].psi0);
+        } else if (ic_on_device(ctx->inst[k])) {
+            on_dev[k] = 1;
         } else {
             rc = build_initial_field(&ctx->inst[k], h + k * n);
             if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
@@ -1219,12 +1324,24 @@ static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) 
     }
     double *dpsi = nullptr;
     XPFC_CUDA(ctx, cudaMallocAsync((void **)&dpsi, sizeof(double) * n * nb, ctx->stream));
-    cudaError_t e = cudaMemcpyAsync(dpsi, h, sizeof(double) * n * nb, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) {
-        rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
-    } else {
-        rc = fail(ctx, XPFC_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    cudaError_t e = cudaSuccess;
+    for (size_t k = 0; k < nb && e == cudaSuccess && rc == XPFC_OK;) {
+        size_t k1 = k + 1;
+        while (k1 < nb && on_dev[k1] == on_dev[k]) k1++;
+        if (on_dev[k]) {
+            for (size_t j = k; j < k1 && rc == XPFC_OK; j++) {
+                std::string why;
+                rc = enqueue_initial_field(ctx->inst[j], dpsi + j * n, ctx->partials, ctx->stream, &why);
+                if (rc != XPFC_OK) fail(ctx, rc, why);
+            }
+        } else {
+            e = cudaMemcpyAsync(dpsi + k * n, h + k * n, sizeof(double) * n * (k1 - k), cudaMemcpyHostToDevice,
+                                ctx->stream);
+        }
+        k = k1;
     }
+    if (e != cudaSuccess) rc = fail(ctx, XPFC_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    if (rc == XPFC_OK) rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
     cudaFreeAsync(dpsi, ctx->stream);
     if (rc != XPFC_OK) return rc;
     XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1322,3 +1439,5 @@ extern "C" int xpfc_batch_get_field(xpfc_batch *b, int i, double *host_psi) {
     }
     return XPFC_OK;
 }
+
+#include "xpfc_server.inc"

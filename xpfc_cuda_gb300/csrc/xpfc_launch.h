@@ -7,6 +7,7 @@
 
 #include "xpfc_kernels.cuh"
 #include "xpfc_regkernels.cuh"
+#include "xpfc_ic.cuh"
 
 namespace xpfc {
 
@@ -38,6 +39,11 @@ cudaError_t launch_convert_f2d(const float *in, double *out, long long n, cudaSt
 // ninst instances: instance z reduces part[z * nparts * nq ...] into out + z * ostride
 cudaError_t launch_finalize(int nq, const double *part, long long nparts, double *out, cudaStream_t s, int ninst = 1,
                             long long ostride = 0);
+
+// initial field on the device, then its mean pinned to a.psi0; scratch holds
+// at least IC_SCRATCH doubles
+constexpr int IC_BLOCKS = 1024, IC_SCRATCH = IC_BLOCKS + 8;
+cudaError_t launch_initial_field(const ICArgs &a, double *psi, double *scratch, cudaStream_t s);
 
 // grid shapes the launchers use (for sizing the partials buffer)
 int row_rows(int L);
