@@ -16,6 +16,11 @@ rank advances its own independent solve; no collective on the data path).
 --impl reference: the CPU implementation of the same step (the FP64 oracle
 restating the reference's loop, OpenMP on the host cores), rank 0 only.
 
+Two more legs ride on the same line: "sweep" (64 independent solves of
+1000 steps through one xpfc_batch: solves/s, against the same solves one
+context at a time) and "serve" (a Poisson stream of solve requests through
+xpfc_server: latency percentiles and served grid-point-steps/s).
+
 Prints one JSON line on rank 0.
 """
 import argparse
@@ -227,6 +232,49 @@ def run_sweep(args, rank, local, group, barrier):
     return out
 
 
+def run_serve(args, rank, local, group, barrier):
+    """Serving loop (xpfc_server) on a Poisson request stream: latency
+    percentiles and served throughput."""
+    import numpy as np
+
+    import xpfc_cuda_gb300 as X
+    from xpfc_cuda_gb300 import serving as SV
+    rate = 20.0
+    stream = SV.request_stream(args.serve_requests, rate=rate, seed=rank, device=local)
+    # a few of the smaller requests keep their fields for the same-as-alone check
+    keep = [i for i, (_, p, k) in enumerate(stream) if p.Mx <= 96 and k <= 2000][:3]
+    budget = 150 << 30
+    with X.Server(hbm_budget_bytes=budget, max_running=args.serve_running, chunk_steps=16, device=local) as srv:
+        # warm server: one short solve of every size (kernel modules loaded, one
+        # pooled context per size)
+        warm = [srv.submit(p, 3) for p in {p.Mx: p for _, p, _ in stream}.values()]
+        for w in warm:
+            srv.wait(w)
+        barrier()
+        ids, recs, span = SV.play(srv, stream, set(keep))
+        barrier()
+        stats = srv.stats()
+        same = True
+        for i in keep:
+            _, p, k = stream[i]
+            f, r = srv.result(ids[i], shape=(p.Mx, p.My, p.Mz))
+            with X.Xpfc(p) as x:
+                x.initialize(None)
+                r1 = x.step(k)
+                f1 = x.copy2cpu()
+            same &= bool(np.array_equal(f, f1) and r == r1)
+    out = SV.summarise(recs, span, rate)
+    out.update({"unit": "s", "rate_per_s": rate, "max_running": args.serve_running, "chunk_steps": 16,
+                "hbm_budget_gb": budget / 2 ** 30, "peak_device_gb": stats["peak_bytes_in_use"] / 2 ** 30,
+                "contexts_created": stats["contexts_created"], "contexts_reused": stats["contexts_reused"],
+                "same_as_alone_checked": len(keep), "same_as_alone": same,
+                "workload": "%d requests, Poisson 20/s, N^3 with N in (64,96,128,192,256) w=(.3,.25,.2,.15,.1), "
+                            "steps U[200,5000], sweep physics, FP32 bulk, device initial fields" % len(stream),
+                "timed": "wall clock from the first arrival to the last completion; per-request times from the "
+                         "server's clock (submit, admit, done)"})
+    return out
+
+
 def run_ours(args):
     import torch
     import numpy as np
@@ -357,13 +405,17 @@ def run_ours(args):
         torch.cuda.set_stream(torch.cuda.default_stream())
         sweep = run_sweep(args, rank, local, group, barrier)
 
+    serve = None
+    if not args.no_serve:
+        serve = run_serve(args, rank, local, group, barrier)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == X._lib.MIXED else "f64",
                 "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, args.precision),
                 "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
-                "fp64": fp64, "sweep": sweep}
+                "fp64": fp64, "sweep": sweep, "serve": serve}
         print(json.dumps(line), flush=True)
     x.close()
     group.close()
@@ -386,6 +438,9 @@ def main():
     ap.add_argument("--no-sweep-seq", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=64)
     ap.add_argument("--sweep-steps", type=int, default=1000)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--serve-running", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
