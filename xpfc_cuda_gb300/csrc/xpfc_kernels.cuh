@@ -316,20 +316,38 @@ struct KSpace {
 
 template <typename T> struct Coef { T A, B, c2, k2; };
 
+// This block's instance (grid z) of a batched launch: its coefficient table
+// and noise seed, resolved once per block so that the per-mode code does not
+// see the batch.
+struct Inst {
+    const void *table;
+    unsigned long long seed;
+};
+template <typename T>
+__device__ __forceinline__ Inst inst_of(const KSpace &k) {
+    Inst r;
+    r.table = k.table;
+    r.seed = k.noise_seed;
+    if (k.tstride && k.table)
+        r.table = reinterpret_cast<const char *>(k.table) + (size_t)blockIdx.z * k.tstride * 4 * sizeof(T);
+    if (k.seeds) r.seed = k.seeds[blockIdx.z];
+    return r;
+}
+
 __device__ __forceinline__ int signed_idx(int i, int n) { return 2 * i <= n ? i : i - n; }
 
 template <typename T>
-__device__ __forceinline__ Coef<T> kcoef(const KSpace &ks, int i0, int i1, int i2) {
+__device__ __forceinline__ Coef<T> kcoef(const KSpace &ks, const void *table, int i0, int i1, int i2) {
     const int s1 = signed_idx(i1, ks.n1), s2 = signed_idx(i2, ks.n2);
     Coef<T> r;
-    if (ks.table) {
-        const long long m = (long long)blockIdx.z * ks.tstride + (i0 * i0 + s1 * s1 + s2 * s2);
+    if (table) {
+        const int m = i0 * i0 + s1 * s1 + s2 * s2;
         if constexpr (sizeof(T) == 4) {
-            const float4 e = __ldg(reinterpret_cast<const float4 *>(ks.table) + m);
+            const float4 e = __ldg(reinterpret_cast<const float4 *>(table) + m);
             r.A = e.x; r.B = e.y; r.c2 = e.z; r.k2 = e.w;
         } else {
-            const double2 e0 = __ldg(reinterpret_cast<const double2 *>(ks.table) + 2 * (size_t)m);
-            const double2 e1 = __ldg(reinterpret_cast<const double2 *>(ks.table) + 2 * (size_t)m + 1);
+            const double2 e0 = __ldg(reinterpret_cast<const double2 *>(table) + 2 * (size_t)m);
+            const double2 e1 = __ldg(reinterpret_cast<const double2 *>(table) + 2 * (size_t)m + 1);
             r.A = e0.x; r.B = e0.y; r.c2 = e1.x; r.k2 = e1.y;
         }
         return r;
@@ -380,7 +398,8 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T &g0, T &g1)
 // Philox draw for a canonical mode (c0, c1, c2): the slowest axis (z in 3-D,
 // y in 2-D) is folded in half; the lower half takes outputs 0,1, the upper 2,3.
 template <bool ROLLED = true>
-__device__ __forceinline__ uint4 noise_draw(const KSpace &ks, int c0, int c1, int c2, bool &upper) {
+__device__ __forceinline__ uint4 noise_draw(const KSpace &ks, unsigned long long seed, int c0, int c1, int c2,
+                                            bool &upper) {
     long long ctr;
     if (ks.n2 > 1) {
         upper = 2 * c2 >= ks.n2;
@@ -390,7 +409,6 @@ __device__ __forceinline__ uint4 noise_draw(const KSpace &ks, int c0, int c1, in
         ctr = (long long)(c1 % (ks.n1 / 2)) * ks.n0 + c0;
     }
     const unsigned long long stream = 1ull + (unsigned long long)ks.step;
-    const unsigned long long seed = ks.seeds ? ks.seeds[blockIdx.z] : ks.noise_seed;
     return philox4x32_10<ROLLED>(make_uint4((uint32_t)ctr, (uint32_t)((unsigned long long)ctr >> 32), (uint32_t)stream,
                                             (uint32_t)(stream >> 32)),
                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
@@ -403,14 +421,14 @@ template <typename T> __device__ __forceinline__ T noise_amp_of(const KSpace &ks
 // conserved noise xi_k = amp sqrt(cells) |k| g_k at full-grid mode (i0,i1,i2),
 // i0 in [0, n0/2]; Hermitian pairing as the oracle defines it
 template <typename T>
-__device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, int i0, int i1, int i2, T k2) {
+__device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, unsigned long long seed, int i0, int i1, int i2, T k2) {
     const int j1 = (ks.n1 - i1) % ks.n1, j2 = (ks.n2 - i2) % ks.n2;
     const bool edge = (i0 == 0) || (2 * i0 == ks.n0);
     const bool selfc = edge && j1 == i1 && j2 == i2;
     bool canon = true;
     if (edge) canon = (long long)i2 * ks.n1 + i1 <= (long long)j2 * ks.n1 + j1;
     bool upper;
-    const uint4 o = canon ? noise_draw(ks, i0, i1, i2, upper) : noise_draw(ks, i0, j1, j2, upper);
+    const uint4 o = canon ? noise_draw(ks, seed, i0, i1, i2, upper) : noise_draw(ks, seed, i0, j1, j2, upper);
     T g0, g1;
     box_muller<T>(upper ? o.z : o.x, upper ? o.w : o.y, g0, g1);
     const T amp = noise_amp_of<T>(ks, k2);
@@ -422,10 +440,10 @@ __device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, int i0, int i1, in
 // Noise of two interior modes (0 < i0 < n0/2) whose slow coordinates are s
 // and s + n_slow/2: one Philox call, both halves of its output.
 template <typename T>
-__device__ __forceinline__ void noise_pair_interior(const KSpace &ks, int i0, int i1, int i2, T k2a, T k2b,
-                                                    cplx<T> &na, cplx<T> &nb) {
+__device__ __forceinline__ void noise_pair_interior(const KSpace &ks, unsigned long long seed, int i0, int i1, int i2,
+                                                    T k2a, T k2b, cplx<T> &na, cplx<T> &nb) {
     bool upper;
-    const uint4 o = noise_draw<false>(ks, i0, i1, i2, upper);
+    const uint4 o = noise_draw<false>(ks, seed, i0, i1, i2, upper);
     T g0, g1, g2, g3;
     box_muller<T>(o.x, o.y, g0, g1);
     box_muller<T>(o.z, o.w, g2, g3);
@@ -466,6 +484,7 @@ __device__ __forceinline__ double pin_of(const PenArgs &a) {
 template <typename T, int L, int NG>
 __global__ void __launch_bounds__(PenShape<T, L, NG>::THREADS)
 pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
+    const Inst in = inst_of<T>(ks);
     using S = PenShape<T, L, NG>;
     constexpr int TX = S::TX, TPL = S::TPL;
     constexpr int TILE = L * TX;
@@ -524,9 +543,9 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
         const cplx<T> xw = tiles[(1 * NG + g) * TILE + kz * TX + c];
         cplx<T> out;
         if (slot != 0) {
-            Coef<T> cf = kcoef<T>(ks, slot, i1, i2);
+            Coef<T> cf = kcoef<T>(ks, in.table, slot, i1, i2);
             cplx<T> num = xs;
-            if (ks.noise_on) num = cadd(num, noise_at<T>(ks, slot, i1, i2, cf.k2));
+            if (ks.noise_on) num = cadd(num, noise_at<T>(ks, in.seed, slot, i1, i2, cf.k2));
             cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
             if (args.want_red) {
                 const double xr = xs.x, xi = xs.y;
@@ -547,11 +566,11 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
             // X0 = (P + conj Pm)/2, XN = (P - conj Pm)/(2i) = -i (P - conj Pm)/2
             const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
             const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
-            const Coef<T> c0 = kcoef<T>(ks, 0, i1, i2), cN = kcoef<T>(ks, nh, i1, i2);
+            const Coef<T> c0 = kcoef<T>(ks, in.table, 0, i1, i2), cN = kcoef<T>(ks, in.table, nh, i1, i2);
             cplx<T> num0 = s0, numN = sN;
             if (ks.noise_on) {
-                num0 = cadd(num0, noise_at<T>(ks, 0, i1, i2, c0.k2));
-                numN = cadd(numN, noise_at<T>(ks, nh, i1, i2, cN.k2));
+                num0 = cadd(num0, noise_at<T>(ks, in.seed, 0, i1, i2, c0.k2));
+                numN = cadd(numN, noise_at<T>(ks, in.seed, nh, i1, i2, cN.k2));
             }
             cplx<T> x0n = mk<T>(c0.A * num0.x + c0.B * w0.x, c0.A * num0.y + c0.B * w0.y);
             cplx<T> xNn = mk<T>(cN.A * numN.x + cN.B * wN.x, cN.A * numN.y + cN.B * wN.y);
@@ -678,7 +697,7 @@ enum { KOP_EULER = 0, KOP_CONVOLVE = 1, KOP_RESIDUAL = 2 };
 template <typename T, int OP>
 __device__ __forceinline__ cplx<T> kop(const KSpace &ks, double a, double b, int i0, int i1, int i2, cplx<T> x1,
                                         cplx<T> x2, cplx<T> x3, cplx<T> x4) {
-    const Coef<T> cf = kcoef<T>(ks, i0, i1, i2);
+    const Coef<T> cf = kcoef<T>(ks, ks.table, i0, i1, i2);
     const T k2 = cf.k2, c2 = cf.c2, dt = (T)ks.dt, Mo = (T)ks.Mo;
     if (OP == KOP_EULER) {
         // euler_step.cu:50-59

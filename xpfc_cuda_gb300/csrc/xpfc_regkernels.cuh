@@ -278,11 +278,11 @@ __device__ __forceinline__ cplx<T> update_coef(const KSpace &ks, const Coef<T> &
 }
 
 template <typename T>
-__device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const PenArgs &args, int i0, int i1, int i2,
-                                               cplx<T> xs, cplx<T> xw, DSum<T, NQ_PEN> &acc, T weight) {
-    const Coef<T> cf = kcoef<T>(ks, i0, i1, i2);
+__device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const Inst &in, const PenArgs &args, int i0, int i1,
+                                               int i2, cplx<T> xs, cplx<T> xw, DSum<T, NQ_PEN> &acc, T weight) {
+    const Coef<T> cf = kcoef<T>(ks, in.table, i0, i1, i2);
     cplx<T> noise = mk<T>((T)0, (T)0);
-    if (ks.noise_on) noise = noise_at<T>(ks, i0, i1, i2, cf.k2);
+    if (ks.noise_on) noise = noise_at<T>(ks, in.seed, i0, i1, i2, cf.k2);
     const cplx<T> num = cadd(xs, noise);
     cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
     if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)pin_of(args), (T)0);
@@ -293,6 +293,7 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const PenArgs &
 template <typename T, int N, int NG, bool RED>
 __global__ void __launch_bounds__(RPenShape<T, N, NG>::THREADS, RPenShape<T, N, NG>::MINB)
 pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
+    const Inst in = inst_of<T>(ks);
     using S = RPenShape<T, N, NG>;
     constexpr int TX = S::TX, Q = S::Q, P = S::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -358,8 +359,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const T h = (T)0.5;
             const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
             const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
-            const cplx<T> x0 = update_mode<T>(ks, args, 0, i1, i2, s0, w0, acc, (T)1);
-            const cplx<T> xN = update_mode<T>(ks, args, nh, i1, i2, sN, wN, acc, (T)1);
+            const cplx<T> x0 = update_mode<T>(ks, in, args, 0, i1, i2, s0, w0, acc, (T)1);
+            const cplx<T> xN = update_mode<T>(ks, in, args, nh, i1, i2, sN, wN, acc, (T)1);
             outS[gg * N + kz] = cscale(cadd(x0, cmuli<1>(xN)), sc);
         }
         __syncthreads();
@@ -377,9 +378,9 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const int kza = t + Q * j, kzb = kza + N / 2;
             const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
             const int i1b = args.three_d ? yg : kzb, i2b = args.three_d ? kzb : 0;
-            const Coef<T> ca = kcoef<T>(ks, i0, i1a, i2a), cb = kcoef<T>(ks, i0, i1b, i2b);
+            const Coef<T> ca = kcoef<T>(ks, in.table, i0, i1a, i2a), cb = kcoef<T>(ks, in.table, i0, i1b, i2b);
             cplx<T> na = zero, nb = zero;
-            if (ks.noise_on) noise_pair_interior<T>(ks, i0, i1a, i2a, ca.k2, cb.k2, na, nb);
+            if (ks.noise_on) noise_pair_interior<T>(ks, in.seed, i0, i1a, i2a, ca.k2, cb.k2, na, nb);
             vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, (T)2), sc);
             vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, (T)2), sc);
         }
