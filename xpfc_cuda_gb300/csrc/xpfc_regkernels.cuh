@@ -369,10 +369,32 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             for (int j = 0; j < P; j++) vs[j] = outS[g * N + t + Q * j];
         }
     }
-    if (valid && kx0 + c != 0) {
-        // interior columns: modes j and j + P/2 sit at kz and kz + N/2 and
-        // share one Philox draw
-        const int i0 = kx0 + c;
+    // interior columns: modes j and j + P/2 sit at kz and kz + N/2 and share
+    // one Philox draw.  The draws are made first, in a rolled loop, into
+    // shared memory (bufS is free between the two transforms; each thread
+    // reads back only its own entries), so that the Philox and Box-Muller code
+    // appears once in the instruction stream instead of P/2 times.
+    const bool interior = valid && kx0 + c != 0;
+    const int i0 = kx0 + c;
+    cplx<T> *snoise = bufS;
+    static_assert(P * S::THREADS <= S::LINES * S::LP, "noise staging must fit in bufS");
+    if (ks.noise_on) {
+        __syncthreads();   // the forward transform and the slot-0 pass are done with bufS
+        if (interior) {
+#pragma unroll 1
+            for (int j = 0; j < P / 2; j++) {
+                const int kza = t + Q * j, kzb = kza + N / 2;
+                const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
+                const int i1b = args.three_d ? yg : kzb, i2b = args.three_d ? kzb : 0;
+                const T k2a = kcoef<T>(ks, in.table, i0, i1a, i2a).k2, k2b = kcoef<T>(ks, in.table, i0, i1b, i2b).k2;
+                cplx<T> na, nb;
+                noise_pair_interior<T>(ks, in.seed, i0, i1a, i2a, k2a, k2b, na, nb);
+                snoise[j * S::THREADS + tid] = na;
+                snoise[(j + P / 2) * S::THREADS + tid] = nb;
+            }
+        }
+    }
+    if (interior) {
 #pragma unroll
         for (int j = 0; j < P / 2; j++) {
             const int kza = t + Q * j, kzb = kza + N / 2;
@@ -380,7 +402,10 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const int i1b = args.three_d ? yg : kzb, i2b = args.three_d ? kzb : 0;
             const Coef<T> ca = kcoef<T>(ks, in.table, i0, i1a, i2a), cb = kcoef<T>(ks, in.table, i0, i1b, i2b);
             cplx<T> na = zero, nb = zero;
-            if (ks.noise_on) noise_pair_interior<T>(ks, in.seed, i0, i1a, i2a, ca.k2, cb.k2, na, nb);
+            if (ks.noise_on) {
+                na = snoise[j * S::THREADS + tid];
+                nb = snoise[(j + P / 2) * S::THREADS + tid];
+            }
             vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, (T)2), sc);
             vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, (T)2), sc);
         }
