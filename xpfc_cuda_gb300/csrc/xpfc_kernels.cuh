@@ -371,9 +371,18 @@ __device__ __forceinline__ Coef<T> kcoef(const KSpace &ks, const void *table, in
     return r;
 }
 
+// Square root through the hardware approximation (relative error about
+// 2^-23): enough for noise amplitudes, one instruction instead of the
+// correctly rounded sequence.
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Box-Muller of two 32-bit draws: u1 = (a+1) 2^-32 in (0,1], u2 = b 2^-32.
-// FP32 uses the hardware log/sin/cos approximations (the noise only needs
-// its distribution); FP64 the accurate functions.
+// FP32 uses the hardware log/sqrt/sin/cos approximations (the noise only
+// needs its distribution); FP64 the accurate functions.
 template <typename T>
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T &g0, T &g1) {
     if (sizeof(T) == 8) {
@@ -387,7 +396,7 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T &g0, T &g1)
     } else {
         const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
         const float u2 = (float)b * 2.3283064365386963e-10f;
-        const float rr = sqrtf(-2.0f * __logf(u1));
+        const float rr = sqrt_approx(fmaxf(0.0f, -2.0f * __logf(u1)));
         float sn, cs;
         __sincosf(6.28318530717958647692f * u2, &sn, &cs);
         g0 = (T)(rr * cs);
@@ -400,22 +409,26 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T &g0, T &g1)
 template <bool ROLLED = true>
 __device__ __forceinline__ uint4 noise_draw(const KSpace &ks, unsigned long long seed, int c0, int c1, int c2,
                                             bool &upper) {
-    long long ctr;
+    // the counter is below n0 n1 n2 / 2, which fits in 32 bits for every
+    // supported grid (at most 2^27 cells), so its upper word is 0
+    uint32_t ctr;
     if (ks.n2 > 1) {
         upper = 2 * c2 >= ks.n2;
-        ctr = ((long long)(c2 % (ks.n2 / 2)) * ks.n1 + c1) * ks.n0 + c0;
+        const int f2 = upper ? c2 - ks.n2 / 2 : c2;
+        ctr = ((uint32_t)f2 * (uint32_t)ks.n1 + (uint32_t)c1) * (uint32_t)ks.n0 + (uint32_t)c0;
     } else {
         upper = 2 * c1 >= ks.n1;
-        ctr = (long long)(c1 % (ks.n1 / 2)) * ks.n0 + c0;
+        const int f1 = upper ? c1 - ks.n1 / 2 : c1;
+        ctr = (uint32_t)f1 * (uint32_t)ks.n0 + (uint32_t)c0;
     }
     const unsigned long long stream = 1ull + (unsigned long long)ks.step;
-    return philox4x32_10<ROLLED>(make_uint4((uint32_t)ctr, (uint32_t)((unsigned long long)ctr >> 32), (uint32_t)stream,
-                                            (uint32_t)(stream >> 32)),
+    return philox4x32_10<ROLLED>(make_uint4(ctr, 0u, (uint32_t)stream, (uint32_t)(stream >> 32)),
                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
 }
 
 template <typename T> __device__ __forceinline__ T noise_amp_of(const KSpace &ks, T k2) {
-    return (sizeof(T) == 4 ? (T)ks.f_noise_scale : (T)ks.noise_scale) * sqrt(k2);
+    if constexpr (sizeof(T) == 4) return ks.f_noise_scale * sqrt_approx(k2);
+    else return (T)ks.noise_scale * sqrt(k2);
 }
 
 // conserved noise xi_k = amp sqrt(cells) |k| g_k at full-grid mode (i0,i1,i2),
@@ -437,20 +450,21 @@ __device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, unsigned long long
     return mk<T>(amp * g0 * h, (canon ? amp : -amp) * g1 * h);
 }
 
-// Noise of two interior modes (0 < i0 < n0/2) whose slow coordinates are s
-// and s + n_slow/2: one Philox call, both halves of its output.
+// Unit-amplitude noise of two interior modes (0 < i0 < n0/2) whose slow
+// coordinates are s and s + n_slow/2: one Philox call, both halves of its
+// output, each complex Gaussian scaled by 1/sqrt 2 (the mode amplitude
+// noise_amp_of(k^2) multiplies it where the coefficients are at hand).
 template <typename T>
-__device__ __forceinline__ void noise_pair_interior(const KSpace &ks, unsigned long long seed, int i0, int i1, int i2,
-                                                    T k2a, T k2b, cplx<T> &na, cplx<T> &nb) {
+__device__ __forceinline__ void noise_pair_unit(const KSpace &ks, unsigned long long seed, int i0, int i1, int i2,
+                                                cplx<T> &ga, cplx<T> &gb) {
     bool upper;
     const uint4 o = noise_draw<false>(ks, seed, i0, i1, i2, upper);
     T g0, g1, g2, g3;
     box_muller<T>(o.x, o.y, g0, g1);
     box_muller<T>(o.z, o.w, g2, g3);
     const T h = (T)0.70710678118654752440;
-    const T a = noise_amp_of<T>(ks, k2a) * h, b = noise_amp_of<T>(ks, k2b) * h;
-    na = mk<T>(a * g0, a * g1);
-    nb = mk<T>(b * g2, b * g3);
+    ga = mk<T>(h * g0, h * g1);
+    gb = mk<T>(h * g2, h * g3);
 }
 
 // ---------------------------------------------------------------------------

@@ -383,14 +383,12 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
         if (interior) {
 #pragma unroll 1
             for (int j = 0; j < P / 2; j++) {
-                const int kza = t + Q * j, kzb = kza + N / 2;
+                const int kza = t + Q * j;
                 const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
-                const int i1b = args.three_d ? yg : kzb, i2b = args.three_d ? kzb : 0;
-                const T k2a = kcoef<T>(ks, in.table, i0, i1a, i2a).k2, k2b = kcoef<T>(ks, in.table, i0, i1b, i2b).k2;
-                cplx<T> na, nb;
-                noise_pair_interior<T>(ks, in.seed, i0, i1a, i2a, k2a, k2b, na, nb);
-                snoise[j * S::THREADS + tid] = na;
-                snoise[(j + P / 2) * S::THREADS + tid] = nb;
+                cplx<T> ga, gb;
+                noise_pair_unit<T>(ks, in.seed, i0, i1a, i2a, ga, gb);
+                snoise[j * S::THREADS + tid] = ga;
+                snoise[(j + P / 2) * S::THREADS + tid] = gb;
             }
         }
     }
@@ -403,8 +401,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const Coef<T> ca = kcoef<T>(ks, in.table, i0, i1a, i2a), cb = kcoef<T>(ks, in.table, i0, i1b, i2b);
             cplx<T> na = zero, nb = zero;
             if (ks.noise_on) {
-                na = snoise[j * S::THREADS + tid];
-                nb = snoise[(j + P / 2) * S::THREADS + tid];
+                na = cscale(snoise[j * S::THREADS + tid], noise_amp_of<T>(ks, ca.k2));
+                nb = cscale(snoise[(j + P / 2) * S::THREADS + tid], noise_amp_of<T>(ks, cb.k2));
             }
             vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, (T)2), sc);
             vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, (T)2), sc);
