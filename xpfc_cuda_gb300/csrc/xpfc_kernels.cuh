@@ -380,6 +380,12 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     return r;
 }
 
+__device__ __forceinline__ float lg2_approx(float x) {
+    float r;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Box-Muller of two 32-bit draws: u1 = (a+1) 2^-32 in (0,1], u2 = b 2^-32.
 // FP32 uses the hardware log/sqrt/sin/cos approximations (the noise only
 // needs its distribution); FP64 the accurate functions.
@@ -395,13 +401,23 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T &g0, T &g1)
         g1 = (T)(rr * sn);
     } else {
         const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
-        const float u2 = (float)b * 2.3283064365386963e-10f;
-        const float rr = sqrt_approx(fmaxf(0.0f, -2.0f * __logf(u1)));
+        const float rr = sqrt_approx(fmaxf(0.0f, -1.38629436111989061883f * lg2_approx(u1)));   // -2 ln u1
         float sn, cs;
-        __sincosf(6.28318530717958647692f * u2, &sn, &cs);
+        __sincosf((float)b * 1.46291807926715968e-09f, &sn, &cs);   // 2 pi b 2^-32
         g0 = (T)(rr * cs);
         g1 = (T)(rr * sn);
     }
+}
+
+// The same pair scaled by 1/sqrt 2 (the Hermitian split of a complex mode):
+// sqrt(-2 ln u1)/sqrt 2 = sqrt(-ln u1), folded into the radius.
+__device__ __forceinline__ void box_muller_half(uint32_t a, uint32_t b, float &g0, float &g1) {
+    const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
+    const float rr = sqrt_approx(fmaxf(0.0f, -0.69314718055994530942f * lg2_approx(u1)));   // -ln u1
+    float sn, cs;
+    __sincosf((float)b * 1.46291807926715968e-09f, &sn, &cs);
+    g0 = rr * cs;
+    g1 = rr * sn;
 }
 
 // Philox draw for a canonical mode (c0, c1, c2): the slowest axis (z in 3-D,
@@ -459,12 +475,20 @@ __device__ __forceinline__ void noise_pair_unit(const KSpace &ks, unsigned long 
                                                 cplx<T> &ga, cplx<T> &gb) {
     bool upper;
     const uint4 o = noise_draw<false>(ks, seed, i0, i1, i2, upper);
-    T g0, g1, g2, g3;
-    box_muller<T>(o.x, o.y, g0, g1);
-    box_muller<T>(o.z, o.w, g2, g3);
-    const T h = (T)0.70710678118654752440;
-    ga = mk<T>(h * g0, h * g1);
-    gb = mk<T>(h * g2, h * g3);
+    if constexpr (sizeof(T) == 4) {
+        float g0, g1, g2, g3;
+        box_muller_half(o.x, o.y, g0, g1);
+        box_muller_half(o.z, o.w, g2, g3);
+        ga = mk<T>(g0, g1);
+        gb = mk<T>(g2, g3);
+    } else {
+        T g0, g1, g2, g3;
+        box_muller<T>(o.x, o.y, g0, g1);
+        box_muller<T>(o.z, o.w, g2, g3);
+        const T h = (T)0.70710678118654752440;
+        ga = mk<T>(h * g0, h * g1);
+        gb = mk<T>(h * g2, h * g3);
+    }
 }
 
 // ---------------------------------------------------------------------------
