@@ -148,7 +148,7 @@ __device__ __forceinline__ void reg_pack(cplx<T> *v, int t, int lane, const cplx
 // RED: this launch also produces the real-space sums (diagnostics steps); a
 // separate instance keeps that code out of the hot loop of the other steps.
 template <typename T, int N, int MODE, bool RED>
-__global__ void __launch_bounds__(RRowShape<T, N>::THREADS)
+__global__ void __launch_bounds__(RRowShape<T, N>::THREADS, sizeof(T) == 4 ? 4 : 1)
 row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__restrict__ tw2N) {
     using S = RRowShape<T, N>;
     constexpr int Q = S::Q, P = S::P;
