@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -64,6 +65,10 @@ struct xpfc_ctx {
     unsigned long long *seeds = nullptr;   // noise_seed_i
     long long zstride = 0;                 // complex elements between instances
     size_t part_per_inst = 0;              // partial-sum doubles per instance
+    // the xy passes of a 3-D step in plane chunks on auxiliary streams
+    int xy_chunks = -1;                    // -1: not chosen yet
+    cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 enum { PASS_PENCIL = 0, PASS_COL_INV = 1, PASS_ROW = 2, PASS_COL_FWD = 3, PASS_RED = 4 };
@@ -454,6 +459,11 @@ extern "C" int xpfc_destroy(xpfc_ctx *ctx) {
     cudaFree(ctx->init_red);
     cudaFree(ctx->pin_values);
     cudaFree(ctx->seeds);
+    for (int k = 0; k < 4; k++) {
+        if (ctx->aux[k]) cudaStreamDestroy(ctx->aux[k]);
+        if (ctx->ev_join[k]) cudaEventDestroy(ctx->ev_join[k]);
+    }
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->hslots) cudaFreeHost(ctx->hslots);
     if (ctx->hstage) cudaFreeHost(ctx->hstage);
     for (int b = 0; b < XPFC_NBUF; b++) cudaFree(ctx->staged[b]);
@@ -733,6 +743,31 @@ static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int wan
     return XPFC_OK;
 }
 
+// How many plane chunks the 3-D xy passes take (1: one launch per pass).
+// A chunk's slab of S and W stays in L2 from the y-inverse pass through the
+// row pass to the y-forward pass, and the chunks run on four auxiliary
+// streams, so the passes of neighbouring chunks overlap on the SMs.
+// XPFC_XY_CHUNKS overrides the choice.
+static int xy_chunk_count(xpfc_ctx *ctx) {
+    if (ctx->xy_chunks >= 0) return ctx->xy_chunks;
+    int c = 1;
+    const size_t slab = ctx->esz * (size_t)ctx->ncells * ctx->nb;
+    if (ctx->three_d && ctx->n2 % 4 == 0 && ctx->n2 >= 64 && slab >= ((size_t)32 << 20)) c = 4;
+    if (const char *e = getenv("XPFC_XY_CHUNKS")) {
+        const int v = atoi(e);
+        if (v >= 1 && ctx->n2 % v == 0) c = v;
+    }
+    if (c > 1) {
+        for (int k = 0; k < 4 && c > 1; k++)
+            if (cudaStreamCreateWithFlags(&ctx->aux[k], cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&ctx->ev_join[k], cudaEventDisableTiming) != cudaSuccess)
+                c = 1;
+        if (c > 1 && cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess) c = 1;
+    }
+    ctx->xy_chunks = c;
+    return c;
+}
+
 template <typename T>
 static int launch_xy_pass(xpfc_ctx *ctx, int want_red, int *nb) {
     const bool dbl = sizeof(T) == 8;
@@ -759,6 +794,36 @@ static int launch_xy_pass(xpfc_ctx *ctx, int want_red, int *nb) {
         cy.ncols = ctx->L0;
         cy.zstride = ctx->zstride;
         cy.nz = ctx->nb;
+        const int nch = (want_red || ctx->profiling) ? 1 : xy_chunk_count(ctx);
+        if (nch > 1) {
+            // chunks of planes (slow index n2), round robin over the auxiliary
+            // streams, between a fork and a join on the context's stream
+            const int per = ctx->n2 / nch;
+            const long long plane = (long long)ctx->n1 * ctx->L0;   // complex elements per plane
+            XPFC_CUDA(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
+            for (int k = 0; k < 4; k++) XPFC_CUDA(ctx, cudaStreamWaitEvent(ctx->aux[k], ctx->ev_fork, 0));
+            for (int c = 0; c < nch; c++) {
+                cudaStream_t s = ctx->aux[c % 4];
+                const long long off = (long long)c * per * plane;
+                ColArgs cc = cy;
+                cc.in = (const cplx<T> *)ctx->S + off;
+                cc.out = (cplx<T> *)ctx->W + off;
+                XPFC_LAUNCH(ctx, launch_col<T>(1, ctx->n1, cc, per, tw1, s));
+                RowArgs rc = ra;
+                rc.in = (const cplx<T> *)ctx->W + off;
+                rc.out = (cplx<T> *)ctx->W + off;
+                rc.nrows = (long long)ctx->n1 * per;
+                rc.scale = 1.0 / ((double)ctx->n0 * ctx->n1);
+                XPFC_LAUNCH(ctx, launch_row<T>(ROW_FUSED, ctx->L0, rc, tw0, tw2, s, nullptr));
+                cc.in = (const cplx<T> *)ctx->W + off;
+                XPFC_LAUNCH(ctx, launch_col<T>(-1, ctx->n1, cc, per, tw1, s));
+            }
+            for (int k = 0; k < 4; k++) {
+                XPFC_CUDA(ctx, cudaEventRecord(ctx->ev_join[k], ctx->aux[k]));
+                XPFC_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_join[k], 0));
+            }
+            return XPFC_OK;
+        }
         {
             ProfScope ps(ctx, PASS_COL_INV);
             XPFC_LAUNCH(ctx, launch_col<T>(1, ctx->n1, cy, ctx->n2, tw1, ctx->stream));
