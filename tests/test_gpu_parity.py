@@ -139,6 +139,26 @@ def test_fused_mixed_within_tolerance(oracle_mod, shape, steps, fcc):
             assert abs(r["mean"] - mean[i]) <= 1e-9
 
 
+@pytest.mark.parametrize("shape,steps", [((48, 48, 48), 60), ((96, 96, 96), 30), ((192, 192, 1), 60),
+                                         ((48, 96, 192), 20)])
+def test_fused_mixed_radix3_sizes(oracle_mod, shape, steps):
+    """The 12- and 24-point register plans (48, 96, 192) on the mixed path,
+    with conserved noise, against the FP64 oracle."""
+    import xpfc_cuda_gb300 as X
+    p, psi0 = _setup(X, oracle_mod, shape, 8.0, steps, 10, X._lib.MIXED, peaks=FCC_PEAKS, noise=0.01, psi0=0.04,
+                     amp=0.05, sigma=0.22)
+    with X.Xpfc(p) as x:
+        x.initialize(psi0)
+        recs = x.step(steps)
+        field = x.copy2cpu()
+    ref, F, mean, rms = oracle_mod.run(oracle_params(oracle_mod, p), psi0, steps, 10)
+    assert rel_l2(field, ref) <= 1e-5
+    for r in recs:
+        i = r["iteration"]
+        if r["F"] is not None:
+            assert abs(r["F"] - F[i]) <= 1e-6 * abs(F[i]), (i, r["F"], F[i])
+
+
 def test_fused_noise_fp64_matches_oracle(oracle_mod):
     import xpfc_cuda_gb300 as X
     p, psi0 = _setup(X, oracle_mod, (32, 32, 32), 8.0, 20, 10, X._lib.FP64, peaks=FCC_PEAKS, noise=0.01,

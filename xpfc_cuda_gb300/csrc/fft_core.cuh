@@ -192,12 +192,64 @@ template <int DIR, typename T> __device__ __forceinline__ void dft3(cplx<T> *v) 
     v[2] = csub(m, ihd);
 }
 
+// cos(2 pi m/24) from the exact angles (m any integer)
+__host__ __device__ constexpr double c24(int m) {
+    m = ((m % 24) + 24) % 24;
+    if (m > 12) m = 24 - m;
+    if (m > 6) return -c24(12 - m);
+    return m == 0 ? 1.0 : m == 1 ? 0.96592582628906828675 : m == 2 ? 0.86602540378443864676
+         : m == 3 ? 0.70710678118654752440 : m == 4 ? 0.5 : m == 5 ? 0.25881904510252076235 : 0.0;
+}
+__host__ __device__ constexpr double s24(int m) { return c24(6 - m); }
+
+// a * W_N^m (W_N = e^{-2 pi i/N} forward, its conjugate inverse) for N | 24;
+// the quarter turns are exact
+template <int N, int DIR, typename T> __device__ __forceinline__ cplx<T> tw24(cplx<T> a, int m) {
+    const int q = ((m % N) + N) % N;
+    if (q == 0) return a;
+    if (4 * q == N) return cmuli<DIR>(a);
+    if (2 * q == N) return mk<T>(-a.x, -a.y);
+    if (4 * q == 3 * N) return cmuli<-DIR>(a);
+    const int e = q * (24 / N);
+    const T c = (T)c24(e), sn = (T)s24(e);
+    return DIR < 0 ? mk<T>(a.x * c + a.y * sn, a.y * c - a.x * sn) : mk<T>(a.x * c - a.y * sn, a.y * c + a.x * sn);
+}
+
+template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<T> *v);
+
+// DFT of length R1 R2 (R1 R2 | 24) from R2-point DFTs, twiddles W^{n1 k2} and
+// R1-point DFTs: n = n1 + R1 n2, k = k2 + R2 k1.
+template <int R1, int R2, int DIR, typename T> __device__ __forceinline__ void dft_mixed(cplx<T> *v) {
+    constexpr int N = R1 * R2;
+    cplx<T> y[N];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; n1++) {
+        cplx<T> c[R2];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; n2++) c[n2] = v[n1 + R1 * n2];
+        dftR<R2, DIR, T>(c);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; k2++) y[n1 * R2 + k2] = tw24<N, DIR, T>(c[k2], n1 * k2);
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < R2; k2++) {
+        cplx<T> c[R1];
+#pragma unroll
+        for (int n1 = 0; n1 < R1; n1++) c[n1] = y[n1 * R2 + k2];
+        dftR<R1, DIR, T>(c);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) v[k2 + R2 * k1] = c[k1];
+    }
+}
+
 template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<T> *v) {
     if constexpr (R == 2) dft2<DIR>(v[0], v[1]);
     else if constexpr (R == 3) dft3<DIR, T>(v);
     else if constexpr (R == 4) dft4<DIR>(v[0], v[1], v[2], v[3]);
     else if constexpr (R == 8) dft8<DIR, T>(v);
+    else if constexpr (R == 12) dft_mixed<3, 4, DIR, T>(v);
     else if constexpr (R == 16) dft16<DIR, T>(v);
+    else if constexpr (R == 24) dft_mixed<3, 8, DIR, T>(v);
     else static_assert(R == 2, "unsupported radix");
 }
 

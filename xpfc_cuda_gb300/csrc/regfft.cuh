@@ -14,9 +14,20 @@
 namespace xpfc {
 
 template <int N> struct RP { static constexpr bool ok = false; static constexpr int P = 1, Q = 1; };
+template <> struct RP<24> { static constexpr bool ok = true; static constexpr int P = 12, Q = 2; };
+template <> struct RP<48> { static constexpr bool ok = true; static constexpr int P = 12, Q = 4; };
 template <> struct RP<64> { static constexpr bool ok = true; static constexpr int P = 8, Q = 8; };
+template <> struct RP<96> { static constexpr bool ok = true; static constexpr int P = 24, Q = 4; };
+template <> struct RP<192> { static constexpr bool ok = true; static constexpr int P = 24, Q = 8; };
 template <> struct RP<128> { static constexpr bool ok = true; static constexpr int P = 16, Q = 8; };
 template <> struct RP<256> { static constexpr bool ok = true; static constexpr int P = 16, Q = 16; };
+
+// The pencil kernel holds two lines (P values each) per thread: in FP64 the
+// 24-value plans would not fit in registers, so those lengths keep the
+// shared-memory kernels there.
+template <typename T, int N> constexpr bool reg_pen_ok() {
+    return RP<N>::ok && (sizeof(T) == 4 || RP<N>::P <= 16);
+}
 
 // Transpose scratch of one line: P rows of QP slots (QP odd: conflict-free
 // column reads), lines LPITCH apart.

@@ -148,7 +148,7 @@ __device__ __forceinline__ void reg_pack(cplx<T> *v, int t, int lane, const cplx
 // RED: this launch also produces the real-space sums (diagnostics steps); a
 // separate instance keeps that code out of the hot loop of the other steps.
 template <typename T, int N, int MODE, bool RED>
-__global__ void __launch_bounds__(RRowShape<T, N>::THREADS, sizeof(T) == 4 ? 4 : 1)
+__global__ void __launch_bounds__(RRowShape<T, N>::THREADS, sizeof(T) == 4 ? (RP<N>::P <= 16 ? 4 : 2) : 1)
 row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__restrict__ tw2N) {
     using S = RRowShape<T, N>;
     constexpr int Q = S::Q, P = S::P;
@@ -231,7 +231,9 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
 // ---------------------------------------------------------------------------
 template <typename T, int N, int NG> struct RPenShape {
     static constexpr int Q = RP<N>::Q, P = RP<N>::P;
-    static constexpr int TX = sizeof(T) == 4 ? 8 : 4;
+    // columns per block: 8 (FP32) for the 16-thread lines; the 4-thread lines
+    // of 96 take 16, so that a block still holds four warps
+    static constexpr int TX = (sizeof(T) == 4 ? 8 : 4) * ((Q == 4 && N >= 96) ? 2 : 1);
     static constexpr int THREADS = TX * Q * NG;
     static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
     static constexpr int LINES = TX * NG;
