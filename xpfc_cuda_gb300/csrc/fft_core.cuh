@@ -200,24 +200,36 @@ __host__ __device__ constexpr double c24(int m) {
     return m == 0 ? 1.0 : m == 1 ? 0.96592582628906828675 : m == 2 ? 0.86602540378443864676
          : m == 3 ? 0.70710678118654752440 : m == 4 ? 0.5 : m == 5 ? 0.25881904510252076235 : 0.0;
 }
-__host__ __device__ constexpr double s24(int m) { return c24(6 - m); }
+// cos(2 pi m/32) from the exact angles (m any integer)
+__host__ __device__ constexpr double c32(int m) {
+    m = ((m % 32) + 32) % 32;
+    if (m > 16) m = 32 - m;
+    if (m > 8) return -c32(16 - m);
+    return m == 0 ? 1.0 : m == 1 ? 0.98078528040323044913 : m == 2 ? 0.92387953251128675613
+         : m == 3 ? 0.83146961230254523708 : m == 4 ? 0.70710678118654752440 : m == 5 ? 0.55557023301960222474
+         : m == 6 ? 0.38268343236508977173 : m == 7 ? 0.19509032201612826785 : 0.0;
+}
+// cos and sin of 2 pi m/N for N dividing 24 or 32
+__host__ __device__ constexpr double cos2pi(int N, int m) { return 24 % N == 0 ? c24(m * (24 / N)) : c32(m * (32 / N)); }
+__host__ __device__ constexpr double sin2pi(int N, int m) {
+    return 24 % N == 0 ? c24(6 - m * (24 / N)) : c32(8 - m * (32 / N));
+}
 
-// a * W_N^m (W_N = e^{-2 pi i/N} forward, its conjugate inverse) for N | 24;
-// the quarter turns are exact
-template <int N, int DIR, typename T> __device__ __forceinline__ cplx<T> tw24(cplx<T> a, int m) {
+// a * W_N^m (W_N = e^{-2 pi i/N} forward, its conjugate inverse) for N
+// dividing 24 or 32; the quarter turns are exact
+template <int N, int DIR, typename T> __device__ __forceinline__ cplx<T> twc(cplx<T> a, int m) {
     const int q = ((m % N) + N) % N;
     if (q == 0) return a;
     if (4 * q == N) return cmuli<DIR>(a);
     if (2 * q == N) return mk<T>(-a.x, -a.y);
     if (4 * q == 3 * N) return cmuli<-DIR>(a);
-    const int e = q * (24 / N);
-    const T c = (T)c24(e), sn = (T)s24(e);
+    const T c = (T)cos2pi(N, q), sn = (T)sin2pi(N, q);
     return DIR < 0 ? mk<T>(a.x * c + a.y * sn, a.y * c - a.x * sn) : mk<T>(a.x * c - a.y * sn, a.y * c + a.x * sn);
 }
 
 template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<T> *v);
 
-// DFT of length R1 R2 (R1 R2 | 24) from R2-point DFTs, twiddles W^{n1 k2} and
+// DFT of length R1 R2 (dividing 24 or 32) from R2-point DFTs, twiddles W^{n1 k2} and
 // R1-point DFTs: n = n1 + R1 n2, k = k2 + R2 k1.
 template <int R1, int R2, int DIR, typename T> __device__ __forceinline__ void dft_mixed(cplx<T> *v) {
     constexpr int N = R1 * R2;
@@ -229,7 +241,7 @@ template <int R1, int R2, int DIR, typename T> __device__ __forceinline__ void d
         for (int n2 = 0; n2 < R2; n2++) c[n2] = v[n1 + R1 * n2];
         dftR<R2, DIR, T>(c);
 #pragma unroll
-        for (int k2 = 0; k2 < R2; k2++) y[n1 * R2 + k2] = tw24<N, DIR, T>(c[k2], n1 * k2);
+        for (int k2 = 0; k2 < R2; k2++) y[n1 * R2 + k2] = twc<N, DIR, T>(c[k2], n1 * k2);
     }
 #pragma unroll
     for (int k2 = 0; k2 < R2; k2++) {
@@ -242,6 +254,28 @@ template <int R1, int R2, int DIR, typename T> __device__ __forceinline__ void d
     }
 }
 
+// 32 = 2 x 16 by decimation in frequency, in place: X[2k] = DFT16(x[n] +
+// x[n+16]), X[2k+1] = DFT16((x[n] - x[n+16]) W32^n); the final interleave is
+// a renaming of registers
+template <int DIR, typename T> __device__ __forceinline__ void dft32(cplx<T> *v) {
+#pragma unroll
+    for (int n = 0; n < 16; n++) {
+        const cplx<T> a = v[n], b = v[n + 16];
+        v[n] = cadd(a, b);
+        v[n + 16] = twc<32, DIR, T>(csub(a, b), n);
+    }
+    dft16<DIR, T>(v);
+    dft16<DIR, T>(v + 16);
+    cplx<T> u[32];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        u[2 * k] = v[k];
+        u[2 * k + 1] = v[16 + k];
+    }
+#pragma unroll
+    for (int k = 0; k < 32; k++) v[k] = u[k];
+}
+
 template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<T> *v) {
     if constexpr (R == 2) dft2<DIR>(v[0], v[1]);
     else if constexpr (R == 3) dft3<DIR, T>(v);
@@ -250,6 +284,7 @@ template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<
     else if constexpr (R == 12) dft_mixed<3, 4, DIR, T>(v);
     else if constexpr (R == 16) dft16<DIR, T>(v);
     else if constexpr (R == 24) dft_mixed<3, 8, DIR, T>(v);
+    else if constexpr (R == 32) dft32<DIR, T>(v);
     else static_assert(R == 2, "unsupported radix");
 }
 

@@ -19,14 +19,18 @@ template <> struct RP<48> { static constexpr bool ok = true; static constexpr in
 template <> struct RP<64> { static constexpr bool ok = true; static constexpr int P = 8, Q = 8; };
 template <> struct RP<96> { static constexpr bool ok = true; static constexpr int P = 24, Q = 4; };
 template <> struct RP<192> { static constexpr bool ok = true; static constexpr int P = 24, Q = 8; };
+template <> struct RP<512> { static constexpr bool ok = true; static constexpr int P = 32, Q = 16; };
 template <> struct RP<128> { static constexpr bool ok = true; static constexpr int P = 16, Q = 8; };
 template <> struct RP<256> { static constexpr bool ok = true; static constexpr int P = 16, Q = 16; };
 
-// The pencil kernel holds two lines (P values each) per thread: in FP64 the
-// 24-value plans would not fit in registers, so those lengths keep the
-// shared-memory kernels there.
+// Which lengths take the register kernels.  The pencil kernel holds two
+// lines (P values each) per thread: FP64 keeps the shared-memory kernels for
+// P above 16 there, and for P above 24 in the one-line row and column passes.
 template <typename T, int N> constexpr bool reg_pen_ok() {
     return RP<N>::ok && (sizeof(T) == 4 || RP<N>::P <= 16);
+}
+template <typename T, int N> constexpr bool reg_line_ok() {
+    return RP<N>::ok && (sizeof(T) == 4 || RP<N>::P <= 24);
 }
 
 // Transpose scratch of one line: P rows of QP slots (QP odd: conflict-free

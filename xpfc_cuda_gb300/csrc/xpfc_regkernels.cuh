@@ -148,7 +148,8 @@ __device__ __forceinline__ void reg_pack(cplx<T> *v, int t, int lane, const cplx
 // RED: this launch also produces the real-space sums (diagnostics steps); a
 // separate instance keeps that code out of the hot loop of the other steps.
 template <typename T, int N, int MODE, bool RED>
-__global__ void __launch_bounds__(RRowShape<T, N>::THREADS, sizeof(T) == 4 ? (RP<N>::P <= 16 ? 4 : 2) : 1)
+__global__ void __launch_bounds__(RRowShape<T, N>::THREADS,
+                                  sizeof(T) == 4 ? (RP<N>::P <= 16 ? 4 : RP<N>::P <= 24 ? 2 : 1) : 1)
 row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__restrict__ tw2N) {
     using S = RRowShape<T, N>;
     constexpr int Q = S::Q, P = S::P;
@@ -239,7 +240,7 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int LINES = TX * NG;
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
     // two resident blocks per SM (128 registers per thread) for the FP32 instances
-    static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256) ? 2 : 1;
+    static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2 : 1;
 };
 
 // k-space sums of one updated mode: weight c2 |X|^2 (free energy) and
