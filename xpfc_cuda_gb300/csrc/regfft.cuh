@@ -24,13 +24,15 @@ template <> struct RP<128> { static constexpr bool ok = true; static constexpr i
 template <> struct RP<256> { static constexpr bool ok = true; static constexpr int P = 16, Q = 16; };
 
 // Which lengths take the register kernels.  The pencil kernel holds two
-// lines (P values each) per thread: FP64 keeps the shared-memory kernels for
-// P above 16 there, and for P above 24 in the one-line row and column passes.
+// lines (P values each) per thread: FP64 keeps the shared-memory kernel for
+// P above 16 there.  The one-line row and column passes keep it for the
+// 32-value plan (512), whose 167 registers leave one block per SM and ran
+// slower than the shared-memory kernel (594 against 405 us at 512^3).
 template <typename T, int N> constexpr bool reg_pen_ok() {
     return RP<N>::ok && (sizeof(T) == 4 || RP<N>::P <= 16);
 }
 template <typename T, int N> constexpr bool reg_line_ok() {
-    return RP<N>::ok && (sizeof(T) == 4 || RP<N>::P <= 24);
+    return RP<N>::ok && RP<N>::P <= 24;
 }
 
 // Transpose scratch of one line: P rows of QP slots (QP odd: conflict-free
