@@ -146,14 +146,19 @@ def run_reference(args):
                       ff_factor=DX ** 3, noise_amp=0.01, noise_seed=11)
     psi = O.ic_noise(n, n, n, 0.04, 0.05, 1)
     O.pin_mean(psi, 0.04)
-    _, psi = O.bench(p, psi, args.warmup)
-    sec, _ = O.bench(p, psi, args.steps)
-    v = n ** 3 * args.steps / sec / 1e9
+    # bounded sample: at most REF_MAX_STEPS timed and 1 warm-up step of the
+    # full-size workload (one 256^3 FP64 step takes ~0.25 s on 16 cores)
+    REF_MAX_STEPS = 40
+    k = max(1, min(args.steps, REF_MAX_STEPS))
+    _, psi = O.bench(p, psi, 1)
+    sec, _ = O.bench(p, psi, k)
+    v = n ** 3 * k / sec / 1e9
     cb = {"value": v, "unit": UNIT, "cores": O.threads(), "kind": "port",
-          "sample": "%d timed steps (+%d warm-up) of the %d^3 workload, FP64 oracle restating the reference "
-                    "loop (main.cu:306-435); the reference itself is CUDA-only" % (args.steps, args.warmup, n)}
+          "sample": "%d timed steps (+1 warm-up) of the %d^3 workload (of the %d requested), FP64 oracle "
+                    "restating the reference loop (main.cu:306-435); the reference itself is CUDA-only"
+                    % (k, n, args.steps)}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+            "steps": k, "warmup": 1, "ms_per_step": 1e3 * sec / k,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, "mixed"),
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
