@@ -101,6 +101,23 @@ def test_fused_fp64_matches_oracle(oracle_mod, shape, steps):
             assert abs(r["rms"] - rms[i]) <= 1e-8 * abs(rms[i]) + 1e-14, (i, r["rms"], rms[i])
 
 
+@pytest.mark.parametrize("shape,steps", [((4096, 4096, 1), 3), ((2048, 512, 1), 6)])
+def test_fused_fp64_large_2d_matches_oracle(oracle_mod, shape, steps):
+    """Large 2-D FP64 grids, whose pencils are one column wide in shared
+    memory (4096) or two (2048)."""
+    import xpfc_cuda_gb300 as X
+    p, psi0 = _setup(X, oracle_mod, shape, 8.0, steps, 3, X._lib.FP64, noise=0.01)
+    with X.Xpfc(p) as x:
+        x.initialize(psi0)
+        recs = x.step(steps)
+        field = x.copy2cpu()
+    ref, F, mean, rms = oracle_mod.run(oracle_params(oracle_mod, p), psi0, steps, 3)
+    assert rel_l2(field, ref) < 1e-10
+    for r in recs:
+        if r["F"] is not None:
+            assert abs(r["F"] - F[r["iteration"]]) <= 1e-11 * abs(F[r["iteration"]])
+
+
 def test_staged_fp64_matches_oracle(oracle_mod):
     import xpfc_cuda_gb300 as X
     p, psi0 = _setup(X, oracle_mod, (32, 32, 1), 8.0, 50, 10, X._lib.FP64)
@@ -140,10 +157,11 @@ def test_fused_mixed_within_tolerance(oracle_mod, shape, steps, fcc):
 
 
 @pytest.mark.parametrize("shape,steps", [((48, 48, 48), 60), ((96, 96, 96), 30), ((192, 192, 1), 60),
-                                         ((48, 96, 192), 20)])
+                                         ((48, 96, 192), 20), ((512, 512, 1), 30), ((1024, 1024, 1), 20),
+                                         ((256, 2048, 1), 10)])
 def test_fused_mixed_radix3_sizes(oracle_mod, shape, steps):
-    """The 12- and 24-point register plans (48, 96, 192) on the mixed path,
-    with conserved noise, against the FP64 oracle."""
+    """The 12- and 24-point register plans (48, 96, 192) and the large 2-D
+    grids on the mixed path, with conserved noise, against the FP64 oracle."""
     import xpfc_cuda_gb300 as X
     p, psi0 = _setup(X, oracle_mod, shape, 8.0, steps, 10, X._lib.MIXED, peaks=FCC_PEAKS, noise=0.01, psi0=0.04,
                      amp=0.05, sigma=0.22)

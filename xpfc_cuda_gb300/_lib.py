@@ -7,7 +7,7 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libxpfc.so")
+LIB_PATH = os.environ.get("XPFC_LIB") or os.path.join(HERE, "_lib", "libxpfc.so")
 
 MAX_PEAKS = 8
 

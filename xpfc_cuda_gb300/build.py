@@ -15,6 +15,13 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libxpfc.so")
+# XPFC_BUILD_CHECKED=1 builds the self-checking diagnostics library instead
+# (every step-kernel access checked against the registered buffers), into
+# its own objects and libxpfc_checked.so
+CHECKED = os.environ.get("XPFC_BUILD_CHECKED") == "1"
+if CHECKED:
+    OUT = os.path.join(OUT, "checked")
+    LIB = os.path.join(HERE, "_lib", "libxpfc_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -25,6 +32,8 @@ def nvcc():
 
 def _units():
     cu = ["-std=c++17", "-O3", "-lineinfo", "-DNDEBUG", "-Xcompiler", "-fPIC,-ffp-contract=off"] + ARCH
+    if CHECKED:
+        cu = cu + ["-DXPFC_CHECKED"]
     return [
         ("launch_f32_p1.o", [nvcc()] + cu + ["-DXPFC_PART=1", "-c", os.path.join(CSRC, "xpfc_launch_f32.cu")]),
         ("launch_f32_p2.o", [nvcc()] + cu + ["-DXPFC_PART=2", "-c", os.path.join(CSRC, "xpfc_launch_f32.cu")]),

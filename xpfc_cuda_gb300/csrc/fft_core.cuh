@@ -18,6 +18,47 @@
 
 namespace xpfc {
 
+// Self-checking build (-DXPFC_CHECKED, a diagnostics build only): every
+// global access of the step kernels is checked against the device buffers
+// the library registered, every shared-memory access against the block's
+// dynamic shared memory; an access outside them is skipped and the first one
+// recorded (site, address, block, thread) for the host to read.
+#ifdef XPFC_CHECKED
+struct XRange {
+    unsigned long long lo, hi;
+};
+static __device__ XRange g_xranges[64];
+static __device__ int g_xnranges;
+static __device__ unsigned long long g_xfault[4];
+static __device__ __noinline__ bool xchk_fail(int site, unsigned long long a) {
+    if (atomicAdd(&g_xfault[0], 1ull) == 0) {
+        g_xfault[1] = (unsigned long long)site;
+        g_xfault[2] = a;
+        g_xfault[3] = ((unsigned long long)blockIdx.x << 32) | ((unsigned long long)blockIdx.y << 16) | threadIdx.x;
+    }
+    return false;
+}
+__device__ __forceinline__ bool xchk_g(const void *p, int bytes, int site) {
+    const unsigned long long a = (unsigned long long)p;
+    for (int i = 0; i < g_xnranges; i++)
+        if (a >= g_xranges[i].lo && a + bytes <= g_xranges[i].hi) return true;
+    return xchk_fail(site, a);
+}
+__device__ __forceinline__ bool xchk_s(const void *p, int bytes, int site) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned int dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    const long long off = (const unsigned char *)p - smem_raw;
+    if (off >= 0 && off + bytes <= (long long)dyn) return true;
+    return xchk_fail(site, (unsigned long long)off);
+}
+#define XG(p, site) xchk_g((p), (int)sizeof(*(p)), (site))
+#define XS(p, site) xchk_s((p), (int)sizeof(*(p)), (site))
+#else
+#define XG(p, site) true
+#define XS(p, site) true
+#endif
+
 template <typename T> struct ctype;
 template <> struct ctype<float> { using type = float2; };
 template <> struct ctype<double> { using type = double2; };
@@ -331,15 +372,18 @@ __host__ __device__ constexpr int max_regs(int L, int TPL) {
     return m;
 }
 
-// Shared-memory index of element e of a line: rows use a skew of one slot
-// per 128 bytes so that stride-R Stockham writes hit distinct banks.
+// Shared-memory index of element e of a line.  ES = ROW_LAYOUT: a row of
+// the row pass, with a skew of one slot per 128 bytes so that stride-R
+// Stockham writes hit distinct banks; ES >= 1: a column of a tile ES columns
+// wide (a one-column tile is plain contiguous storage, without the skew).
+constexpr int ROW_LAYOUT = 0;
 template <typename T, int ES> struct LineIdx {
     static constexpr int SK = (sizeof(cplx<T>) == 8) ? 4 : 3;
     __device__ __forceinline__ static int at(int e) {
-        if constexpr (ES == 1) return e + (e >> SK);
+        if constexpr (ES == ROW_LAYOUT) return e + (e >> SK);
         else return e * ES;
     }
-    __host__ __device__ static constexpr int span(int L) { return ES == 1 ? L + (L >> SK) + 1 : L * ES; }
+    __host__ __device__ static constexpr int span(int L) { return ES == ROW_LAYOUT ? L + (L >> SK) + 1 : L * ES; }
 };
 
 // One Stockham pass of radix R on every line of the block.
@@ -359,8 +403,8 @@ __device__ __forceinline__ void stockham_pass(cplx<T> *line, int t, const cplx<T
             const int k = j % NS;
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                cplx<T> x = line[I::at(j + r * NB)];
-                if (NS > 1 && r > 0) x = twmul<DIR>(x, tw[k * r * TWS]);
+                cplx<T> x = XS(&line[I::at(j + r * NB)], 101) ? line[I::at(j + r * NB)] : mk<T>((T)0, (T)0);
+                if (NS > 1 && r > 0) x = twmul<DIR>(x, XS(&tw[k * r * TWS], 103) ? tw[k * r * TWS] : mk<T>((T)1, (T)0));
                 v[b][r] = x;
             }
             dftR<R, DIR, T>(v[b]);
@@ -374,7 +418,8 @@ __device__ __forceinline__ void stockham_pass(cplx<T> *line, int t, const cplx<T
             const int k = j % NS;
             const int d = (j / NS) * NS * R + k;
 #pragma unroll
-            for (int r = 0; r < R; r++) line[I::at(d + r * NS)] = v[b][r];
+            for (int r = 0; r < R; r++)
+                if (XS(&line[I::at(d + r * NS)], 102)) line[I::at(d + r * NS)] = v[b][r];
         }
     }
     __syncthreads();
@@ -415,7 +460,7 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NQ], double *__re
     if (threadIdx.x < NQ) {
         double s = 0.0;
         for (int w = 0; w < nwarps; w++) s += sred[w * NQ + threadIdx.x];
-        out[threadIdx.x] = s;
+        if (XG(&out[threadIdx.x], 104)) out[threadIdx.x] = s;
     }
 }
 

@@ -25,11 +25,12 @@ template <> struct RP<256> { static constexpr bool ok = true; static constexpr i
 
 // Which lengths take the register kernels.  The pencil kernel holds two
 // lines (P values each) per thread: FP64 keeps the shared-memory kernel for
-// P above 16 there.  The one-line row and column passes keep it for the
-// 32-value plan (512), whose 167 registers leave one block per SM and ran
-// slower than the shared-memory kernel (594 against 405 us at 512^3).
+// P above 16 there, FP32 for P above 24 (the 32-value plan of 512 spilled
+// about 400 bytes per thread).  The one-line row and column passes keep it
+// for the 32-value plan too, whose 167 registers leave one block per SM and
+// ran slower than the shared-memory kernel (594 against 405 us at 512^3).
 template <typename T, int N> constexpr bool reg_pen_ok() {
-    return RP<N>::ok && (sizeof(T) == 4 || RP<N>::P <= 16);
+    return RP<N>::ok && (sizeof(T) == 4 ? RP<N>::P <= 24 : RP<N>::P <= 16);
 }
 template <typename T, int N> constexpr bool reg_line_ok() {
     return RP<N>::ok && RP<N>::P <= 24;
@@ -58,16 +59,18 @@ __device__ __forceinline__ void reg_fft(cplx<T> *v, int t, cplx<T> *buf, const c
     static_assert(P % Q == 0, "P must be a multiple of Q");
     dftR<P, DIR, T>(v);
 #pragma unroll
-    for (int c = 1; c < P; c++) v[c] = twmul<DIR>(v[c], tw[t * c]);
+    for (int c = 1; c < P; c++) v[c] = twmul<DIR>(v[c], XS(&tw[t * c], 207) ? tw[t * c] : mk<T>((T)1, (T)0));
     __syncthreads();
 #pragma unroll
-    for (int c = 0; c < P; c++) buf[c * QP + t] = v[c];
+    for (int c = 0; c < P; c++)
+        if (XS(&buf[c * QP + t], 201)) buf[c * QP + t] = v[c];
     __syncthreads();
     cplx<T> u[P];
 #pragma unroll
     for (int m = 0; m < M; m++)
 #pragma unroll
-        for (int b = 0; b < Q; b++) u[m * Q + b] = buf[(t + Q * m) * QP + b];
+        for (int b = 0; b < Q; b++)
+            u[m * Q + b] = XS(&buf[(t + Q * m) * QP + b], 202) ? buf[(t + Q * m) * QP + b] : mk<T>((T)0, (T)0);
 #pragma unroll
     for (int m = 0; m < M; m++) dftR<Q, DIR, T>(u + m * Q);
 #pragma unroll
@@ -86,22 +89,25 @@ __device__ __forceinline__ void reg_fft2(cplx<T> *v, cplx<T> *w, int t, cplx<T> 
     dftR<P, DIR, T>(w);
 #pragma unroll
     for (int c = 1; c < P; c++) {
-        const cplx<T> tc = tw[t * c];
+        const cplx<T> tc = XS(&tw[t * c], 208) ? tw[t * c] : mk<T>((T)1, (T)0);
         v[c] = twmul<DIR>(v[c], tc);
         w[c] = twmul<DIR>(w[c], tc);
     }
     __syncthreads();
 #pragma unroll
     for (int c = 0; c < P; c++) {
-        bufv[c * QP + t] = v[c];
-        bufw[c * QP + t] = w[c];
+        if (XS(&bufv[c * QP + t], 203) && XS(&bufw[c * QP + t], 204)) {
+            bufv[c * QP + t] = v[c];
+            bufw[c * QP + t] = w[c];
+        }
     }
     __syncthreads();
     cplx<T> u[P];
 #pragma unroll
     for (int m = 0; m < M; m++)
 #pragma unroll
-        for (int b = 0; b < Q; b++) u[m * Q + b] = bufv[(t + Q * m) * QP + b];
+        for (int b = 0; b < Q; b++)
+            u[m * Q + b] = XS(&bufv[(t + Q * m) * QP + b], 205) ? bufv[(t + Q * m) * QP + b] : mk<T>((T)0, (T)0);
 #pragma unroll
     for (int m = 0; m < M; m++) dftR<Q, DIR, T>(u + m * Q);
 #pragma unroll
@@ -111,7 +117,8 @@ __device__ __forceinline__ void reg_fft2(cplx<T> *v, cplx<T> *w, int t, cplx<T> 
 #pragma unroll
     for (int m = 0; m < M; m++)
 #pragma unroll
-        for (int b = 0; b < Q; b++) u[m * Q + b] = bufw[(t + Q * m) * QP + b];
+        for (int b = 0; b < Q; b++)
+            u[m * Q + b] = XS(&bufw[(t + Q * m) * QP + b], 206) ? bufw[(t + Q * m) * QP + b] : mk<T>((T)0, (T)0);
 #pragma unroll
     for (int m = 0; m < M; m++) dftR<Q, DIR, T>(u + m * Q);
 #pragma unroll

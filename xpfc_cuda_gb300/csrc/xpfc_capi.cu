@@ -16,6 +16,78 @@
 
 using namespace xpfc;
 
+#ifdef XPFC_CHECKED
+// Diagnostics build: every device allocation of the library is registered
+// with the launcher units' checker tables.
+#define XPFC_XDECL(t, p)                                                 \
+    extern "C" int xpfc_xcheck_set_##t##_p##p(const void *ranges, int n); \
+    extern "C" int xpfc_xcheck_get_##t##_p##p(unsigned long long *out);
+XPFC_XDECL(f32, 1)
+XPFC_XDECL(f32, 2)
+XPFC_XDECL(f64, 1)
+XPFC_XDECL(f64, 2)
+static std::vector<XRange> g_host_ranges;
+static void xcheck_publish() {
+    const int n = (int)std::min<size_t>(g_host_ranges.size(), 64);
+    xpfc_xcheck_set_f32_p1(g_host_ranges.data(), n);
+    xpfc_xcheck_set_f32_p2(g_host_ranges.data(), n);
+    xpfc_xcheck_set_f64_p1(g_host_ranges.data(), n);
+    xpfc_xcheck_set_f64_p2(g_host_ranges.data(), n);
+}
+static cudaError_t xchk_malloc(void **p, size_t b) {
+    cudaError_t e = ::cudaMalloc(p, b);
+    if (e == cudaSuccess) {
+        g_host_ranges.push_back({(unsigned long long)*p, (unsigned long long)*p + b});
+        xcheck_publish();
+    }
+    return e;
+}
+static cudaError_t xchk_malloc_async(void **p, size_t b, cudaStream_t s) {
+    cudaError_t e = ::cudaMallocAsync(p, b, s);
+    if (e == cudaSuccess) {
+        cudaStreamSynchronize(s);
+        g_host_ranges.push_back({(unsigned long long)*p, (unsigned long long)*p + b});
+        xcheck_publish();
+    }
+    return e;
+}
+static cudaError_t xchk_free(void *p) {
+    for (size_t i = 0; i < g_host_ranges.size(); i++)
+        if (g_host_ranges[i].lo == (unsigned long long)p) {
+            g_host_ranges.erase(g_host_ranges.begin() + i);
+            break;
+        }
+    cudaDeviceSynchronize();
+    xcheck_publish();
+    return ::cudaFree(p);
+}
+extern "C" int xpfc_xcheck_fault(unsigned long long *out) {
+    unsigned long long v[4];
+    int (*get[4])(unsigned long long *) = {xpfc_xcheck_get_f32_p1, xpfc_xcheck_get_f32_p2, xpfc_xcheck_get_f64_p1,
+                                          xpfc_xcheck_get_f64_p2};
+    for (int k = 0; k < 4; k++) {
+        out[4 * k] = out[4 * k + 1] = out[4 * k + 2] = out[4 * k + 3] = 0;
+        if (get[k](v) == 0)
+            for (int j = 0; j < 4; j++) out[4 * k + j] = v[j];
+    }
+    return 0;
+}
+static cudaError_t xchk_free_async(void *p, cudaStream_t s) {
+    cudaStreamSynchronize(s);
+    for (size_t i = 0; i < g_host_ranges.size(); i++)
+        if (g_host_ranges[i].lo == (unsigned long long)p) {
+            g_host_ranges.erase(g_host_ranges.begin() + i);
+            break;
+        }
+    xcheck_publish();
+    return ::cudaFreeAsync(p, s);
+}
+#define cudaFreeAsync(p, s) xchk_free_async((void *)(p), (s))
+#define cudaMalloc(p, b) xchk_malloc((void **)(p), (b))
+#define cudaMallocAsync(p, b, s) xchk_malloc_async((void **)(p), (b), (s))
+#define cudaFree(p) xchk_free((void *)(p))
+#endif
+
 struct xpfc_ctx {
     xpfc_params p;
     int n0, n1, n2, L0, three_d;

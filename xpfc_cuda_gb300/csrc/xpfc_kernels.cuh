@@ -101,7 +101,7 @@ enum { ROW_FWD = 0, ROW_INV = 1, ROW_FUSED = 2, ROW_NL_FWD = 3 };
 // C2R pre-processing of one row (thread t of TPL handles pairs k, L-k)
 template <typename T, int L, int TPL>
 __device__ __forceinline__ void row_unpack(cplx<T> *line, int t, const cplx<T> *__restrict__ tw2) {
-    using I = LineIdx<T, 1>;
+    using I = LineIdx<T, ROW_LAYOUT>;
     for (int k = t; k <= L / 2; k += TPL) {
         if (k == 0) {
             cplx<T> p = line[I::at(0)];
@@ -110,6 +110,7 @@ __device__ __forceinline__ void row_unpack(cplx<T> *line, int t, const cplx<T> *
             continue;
         }
         const int kk = L - k;
+        if (!XS(&line[I::at(k)], 301) || !XS(&line[I::at(kk)], 302) || !XS(&tw2[k], 303)) continue;
         cplx<T> xk = line[I::at(k)], xc = line[I::at(kk)];
         // Z[k] = (Xk + conj X[L-k]) + i (Xk - conj X[L-k]) W^{-k}
         cplx<T> e = cadd(xk, cconj(xc));
@@ -129,7 +130,7 @@ __device__ __forceinline__ void row_unpack(cplx<T> *line, int t, const cplx<T> *
 // R2C post-processing of one row, packing X[L] into slot 0
 template <typename T, int L, int TPL>
 __device__ __forceinline__ void row_pack(cplx<T> *line, int t, const cplx<T> *__restrict__ tw2) {
-    using I = LineIdx<T, 1>;
+    using I = LineIdx<T, ROW_LAYOUT>;
     const T h = (T)0.5;
     for (int k = t; k <= L / 2; k += TPL) {
         if (k == 0) {
@@ -159,7 +160,7 @@ template <typename T, int L, int MODE>
 __global__ void __launch_bounds__(RowShape<L>::THREADS)
 row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restrict__ tw2L) {
     using S = RowShape<L>;
-    using I = LineIdx<T, 1>;
+    using I = LineIdx<T, ROW_LAYOUT>;
     constexpr int SPAN = I::span(L);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);          // L
@@ -169,8 +170,10 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
 
     const int tid = threadIdx.x;
     for (int i = tid; i < L; i += S::THREADS) {
-        stw[i] = twL[i];
-        stw2[i] = tw2L[i];
+        if (XG(&twL[i], 311) && XG(&tw2L[i], 312) && XS(&stw[i], 313) && XS(&stw2[i], 314)) {
+            stw[i] = twL[i];
+            stw2[i] = tw2L[i];
+        }
     }
     pdl_wait();
     const long long row0 = (long long)blockIdx.x * S::ROWS;
@@ -179,7 +182,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
     const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + zoff + row0 * L;
     for (int e = tid; e < nvalid * L; e += S::THREADS) {
         const int r = e / L, c = e - r * L;
-        lines[r * SPAN + I::at(c)] = gin[e];
+        if (XG(&gin[e], 315) && XS(&lines[r * SPAN + I::at(c)], 316)) lines[r * SPAN + I::at(c)] = gin[e];
     }
     __syncthreads();
 
@@ -189,7 +192,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
     if (MODE == ROW_INV || MODE == ROW_FUSED) {
         row_unpack<T, L, S::TPL>(line, t, stw2);
         __syncthreads();
-        line_fft<T, L, +1, S::TPL, 1>(line, t, stw);
+        line_fft<T, L, +1, S::TPL, ROW_LAYOUT>(line, t, stw);
     }
 
     if (MODE == ROW_INV) {
@@ -207,7 +210,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
             cplx<T> z = line[I::at(m)];
             T x0 = z.x, x1 = z.y;
             if (MODE == ROW_FUSED) { x0 *= sc; x1 *= sc; }
-            if (rout && valid) { rout[2 * m] = x0; rout[2 * m + 1] = x1; }
+            if (rout && valid && XG(&rout[2 * m + 1], 317)) { rout[2 * m] = x0; rout[2 * m + 1] = x1; }
             T p20 = powi(x0, 2, args.ref_compat), p21 = powi(x1, 2, args.ref_compat);
             T p30 = powi(x0, 3, args.ref_compat), p31 = powi(x1, 3, args.ref_compat);
             if (args.want_red && valid) {
@@ -223,7 +226,7 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
     }
 
     if (MODE != ROW_INV) {
-        line_fft<T, L, -1, S::TPL, 1>(line, t, stw);
+        line_fft<T, L, -1, S::TPL, ROW_LAYOUT>(line, t, stw);
         row_pack<T, L, S::TPL>(line, t, stw2);
         __syncthreads();
     }
@@ -231,13 +234,13 @@ row_kernel(RowArgs args, const cplx<T> *__restrict__ twL, const cplx<T> *__restr
     cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + zoff + row0 * L;
     for (int e = tid; e < nvalid * L; e += S::THREADS) {
         const int rr = e / L, c = e - rr * L;
-        gout[e] = lines[rr * SPAN + I::at(c)];
+        if (XG(&gout[e], 318) && XS(&lines[rr * SPAN + I::at(c)], 319)) gout[e] = lines[rr * SPAN + I::at(c)];
     }
 }
 
 template <typename T, int L> constexpr size_t row_smem_bytes() {
     using S = RowShape<L>;
-    return sizeof(cplx<T>) * (2 * L + S::ROWS * LineIdx<T, 1>::span(L)) + sizeof(double) * 32 * NQ_ROW;
+    return sizeof(cplx<T>) * (2 * L + S::ROWS * LineIdx<T, ROW_LAYOUT>::span(L)) + sizeof(double) * 32 * NQ_ROW;
 }
 
 // ---------------------------------------------------------------------------
@@ -265,7 +268,8 @@ col_kernel(ColArgs args, const cplx<T> *__restrict__ twL) {
     cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
     cplx<T> *tile = stw + L;
     const int tid = threadIdx.x;
-    for (int i = tid; i < L; i += S::THREADS) stw[i] = twL[i];
+    for (int i = tid; i < L; i += S::THREADS)
+        if (XG(&twL[i], 321) && XS(&stw[i], 322)) stw[i] = twL[i];
     pdl_wait();
     const long long base =
         (long long)blockIdx.x * TX + (long long)blockIdx.y * args.ostride + (long long)blockIdx.z * args.zstride;
@@ -273,16 +277,21 @@ col_kernel(ColArgs args, const cplx<T> *__restrict__ twL) {
     const int c = tid % TX, t = tid / TX;
     const bool cvalid = (int)blockIdx.x * TX + c < args.ncols;
     if (cvalid)
-        for (int e = t; e < L; e += S::TPL) tile[e * TX + c] = gin[e * args.es + c];
+        for (int e = t; e < L; e += S::TPL)
+            if (XG(&gin[e * args.es + c], 323) && XS(&tile[e * TX + c], 324)) tile[e * TX + c] = gin[e * args.es + c];
     __syncthreads();
     line_fft<T, L, DIR, S::TPL, TX>(tile + c, t, stw);
     cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + base;
     const T sc = (T)args.scale;
     if (!cvalid) return;
     if (args.scale != 1.0)
-        for (int e = t; e < L; e += S::TPL) gout[e * args.es + c] = cscale(tile[e * TX + c], sc);
+        for (int e = t; e < L; e += S::TPL) {
+            if (XG(&gout[e * args.es + c], 325)) gout[e * args.es + c] = cscale(tile[e * TX + c], sc);
+        }
     else
-        for (int e = t; e < L; e += S::TPL) gout[e * args.es + c] = tile[e * TX + c];
+        for (int e = t; e < L; e += S::TPL) {
+            if (XG(&gout[e * args.es + c], 326)) gout[e * args.es + c] = tile[e * TX + c];
+        }
 }
 
 template <typename T, int L> constexpr size_t col_smem_bytes() {
@@ -533,7 +542,8 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
     double *sred = reinterpret_cast<double *>(tiles + NT * TILE);
 
     const int tid = threadIdx.x;
-    for (int i = tid; i < L; i += S::THREADS) stw[i] = twL[i];
+    for (int i = tid; i < L; i += S::THREADS)
+        if (XG(&twL[i], 331) && XS(&stw[i], 332)) stw[i] = twL[i];
     pdl_wait();
 
     const int p = blockIdx.y;
@@ -552,7 +562,8 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
             for (int idx = rest; idx < 2 * G * L; idx += NT * TPL) {
                 const int a = idx / (G * L), g = (idx / L) % G, e = idx % L;
                 const long long off = (long long)yg[g] * args.gstride + kx0 + c + (long long)e * args.es;
-                tiles[(a * NG + g) * TILE + e * TX + c] = (a == 0) ? gS[off] : gW[off];
+                if (XS(&tiles[(a * NG + g) * TILE + e * TX + c], 333) && XG(&gS[off], 334) && XG(&gW[off], 335))
+                    tiles[(a * NG + g) * TILE + e * TX + c] = (a == 0) ? gS[off] : gW[off];
             }
     }
     __syncthreads();
@@ -577,6 +588,7 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
         if (slot >= args.L0) continue;
         const int i1 = args.three_d ? yg[g] : kz;
         const int i2 = args.three_d ? kz : 0;
+        if (!XS(&tiles[(1 * NG + g) * TILE + kz * TX + c], 336)) continue;
         const cplx<T> xs = tiles[(0 * NG + g) * TILE + kz * TX + c];
         const cplx<T> xw = tiles[(1 * NG + g) * TILE + kz * TX + c];
         cplx<T> out;
@@ -598,8 +610,10 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
             // slot 0: separate the kx = 0 and kx = n0/2 planes with the mirror mode
             const int gm = (G == 2) ? 1 - g : g;
             const int kzm = (L - kz) % L;
-            const cplx<T> ps = tiles[(0 * NG + gm) * TILE + kzm * TX];
-            const cplx<T> pw = tiles[(1 * NG + gm) * TILE + kzm * TX];
+            const cplx<T> ps = XS(&tiles[(0 * NG + gm) * TILE + kzm * TX], 337) ? tiles[(0 * NG + gm) * TILE + kzm * TX]
+                                                                                : mk<T>((T)0, (T)0);
+            const cplx<T> pw = XS(&tiles[(1 * NG + gm) * TILE + kzm * TX], 338) ? tiles[(1 * NG + gm) * TILE + kzm * TX]
+                                                                                : mk<T>((T)0, (T)0);
             const T h = (T)0.5;
             // X0 = (P + conj Pm)/2, XN = (P - conj Pm)/(2i) = -i (P - conj Pm)/2
             const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
@@ -639,7 +653,7 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
         if (idx >= G * TILE) continue;
         const int g = idx / TILE, kz = (idx / TX) % L, c = idx % TX;
         if (kx0 + c >= args.L0) continue;
-        tiles[(0 * NG + g) * TILE + kz * TX + c] = res[q];
+        if (XS(&tiles[(0 * NG + g) * TILE + kz * TX + c], 339)) tiles[(0 * NG + g) * TILE + kz * TX + c] = res[q];
     }
     __syncthreads();
     // inverse FFT of the state lines: NG TX lines, 2 TPL threads each
@@ -653,7 +667,7 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
             for (int idx = rest; idx < G * L; idx += NT * TPL) {
                 const int g = idx / L, e = idx % L;
                 const long long off = (long long)yg[g] * args.gstride + kx0 + c + (long long)e * args.es;
-                gS[off] = tiles[g * TILE + e * TX + c];
+                if (XG(&gS[off], 340) && XS(&tiles[g * TILE + e * TX + c], 341)) gS[off] = tiles[g * TILE + e * TX + c];
             }
     }
 }
@@ -680,7 +694,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(const double *__restrict_
     for (int q = 0; q < NQ; q++) v[q] = 0.0;
     for (long long b = threadIdx.x; b < nparts; b += blockDim.x)
 #pragma unroll
-        for (int q = 0; q < NQ; q++) v[q] += part[b * NQ + q];
+        for (int q = 0; q < NQ; q++) v[q] += XG(&part[b * NQ + q], 351) ? part[b * NQ + q] : 0.0;
     block_reduce_store<NQ>(v, out, sred);
 }
 

@@ -62,7 +62,8 @@ col_kernel_reg(ColArgs args, const cplx<T> *__restrict__ twN) {
     cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
     cplx<T> *buf = stw + N;
     const int tid = threadIdx.x;
-    for (int i = tid; i < N; i += S::THREADS) stw[i] = twN[i];
+    for (int i = tid; i < N; i += S::THREADS)
+        if (XG(&twN[i], 401) && XS(&stw[i], 402)) stw[i] = twN[i];
     pdl_wait();
     const int c = tid % TX, t = tid / TX;
     const bool cvalid = (int)blockIdx.x * TX + c < args.ncols;
@@ -71,7 +72,9 @@ col_kernel_reg(ColArgs args, const cplx<T> *__restrict__ twN) {
     const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + base;
     cplx<T> v[P];
 #pragma unroll
-    for (int j = 0; j < P; j++) v[j] = cvalid ? gin[(long long)(t + Q * j) * args.es] : mk<T>((T)0, (T)0);
+    for (int j = 0; j < P; j++)
+        v[j] = (cvalid && XG(&gin[(long long)(t + Q * j) * args.es], 403)) ? gin[(long long)(t + Q * j) * args.es]
+                                                                           : mk<T>((T)0, (T)0);
     __syncthreads();
     reg_fft<T, N, DIR>(v, t, buf + c * S::LP, stw);
     if (!cvalid) return;
@@ -79,7 +82,8 @@ col_kernel_reg(ColArgs args, const cplx<T> *__restrict__ twN) {
     const T sc = (T)args.scale;
 #pragma unroll
     for (int j = 0; j < P; j++)
-        gout[(long long)(t + Q * j) * args.es] = (args.scale != 1.0) ? cscale(v[j], sc) : v[j];
+        if (XG(&gout[(long long)(t + Q * j) * args.es], 404))
+            gout[(long long)(t + Q * j) * args.es] = (args.scale != 1.0) ? cscale(v[j], sc) : v[j];
 }
 
 // ---------------------------------------------------------------------------
@@ -160,8 +164,10 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
     double *sred = reinterpret_cast<double *>(buf + S::ROWS * S::LP);
     const int tid = threadIdx.x;
     for (int i = tid; i < N; i += S::THREADS) {
-        stw[i] = twN[i];
-        stw2[i] = tw2N[i];
+        if (XG(&twN[i], 411) && XG(&tw2N[i], 412) && XS(&stw[i], 413) && XS(&stw2[i], 414)) {
+            stw[i] = twN[i];
+            stw2[i] = tw2N[i];
+        }
     }
     pdl_wait();
     const int r = tid / Q, t = tid % Q, lane = tid & 31;
@@ -171,7 +177,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
     const cplx<T> *gin = reinterpret_cast<const cplx<T> *>(args.in) + zoff + row * N + t;
     cplx<T> v[P];
 #pragma unroll
-    for (int j = 0; j < P; j++) v[j] = valid ? gin[Q * j] : mk<T>((T)0, (T)0);
+    for (int j = 0; j < P; j++) v[j] = (valid && XG(&gin[Q * j], 415)) ? gin[Q * j] : mk<T>((T)0, (T)0);
     __syncthreads();
     cplx<T> *line = buf + r * S::LP;
 
@@ -193,7 +199,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
             T x0 = v[j].x, x1 = v[j].y;
             if (MODE == ROW_FUSED) { x0 *= sc; x1 *= sc; }
             const int m = t + Q * j;
-            if (rout && valid) { rout[2 * m] = x0; rout[2 * m + 1] = x1; }
+            if (rout && valid && XG(&rout[2 * m + 1], 416)) { rout[2 * m] = x0; rout[2 * m + 1] = x1; }
             const T p20 = powi(x0, 2, args.ref_compat), p21 = powi(x1, 2, args.ref_compat);
             const T p30 = powi(x0, 3, args.ref_compat), p31 = powi(x1, 3, args.ref_compat);
             if (RED && valid) {
@@ -222,7 +228,8 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
     if (!valid) return;
     cplx<T> *gout = reinterpret_cast<cplx<T> *>(args.out) + zoff + row * N + t;
 #pragma unroll
-    for (int j = 0; j < P; j++) gout[Q * j] = v[j];
+    for (int j = 0; j < P; j++)
+        if (XG(&gout[Q * j], 417)) gout[Q * j] = v[j];
 }
 
 // ---------------------------------------------------------------------------
@@ -305,7 +312,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     cplx<T> *bufW = bufS + S::LINES * S::LP;
     double *sred = reinterpret_cast<double *>(bufW + S::LINES * S::LP);
     const int tid = threadIdx.x;
-    for (int i = tid; i < N; i += S::THREADS) stw[i] = twN[i];
+    for (int i = tid; i < N; i += S::THREADS)
+        if (XG(&twN[i], 421) && XS(&stw[i], 422)) stw[i] = twN[i];
     pdl_wait();
 
     const int c = tid % TX, t = (tid / TX) % Q, g = tid / (TX * Q);
@@ -322,8 +330,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
 #pragma unroll
     for (int j = 0; j < P; j++) {
         const long long e = (long long)(t + Q * j) * args.es;
-        vs[j] = valid ? gS[e] : mk<T>((T)0, (T)0);
-        vw[j] = valid ? gW[e] : mk<T>((T)0, (T)0);
+        vs[j] = (valid && XG(&gS[e], 423)) ? gS[e] : mk<T>((T)0, (T)0);
+        vw[j] = (valid && XG(&gW[e], 424)) ? gW[e] : mk<T>((T)0, (T)0);
     }
     __syncthreads();
     const int ln = g * TX + c;
@@ -344,8 +352,10 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
         if (c == 0 && g < G) {
 #pragma unroll
             for (int j = 0; j < P; j++) {
-                bufS[g * N + t + Q * j] = vs[j];
-                bufW[g * N + t + Q * j] = vw[j];
+                if (XS(&bufS[g * N + t + Q * j], 425) && XS(&bufW[g * N + t + Q * j], 426)) {
+                    bufS[g * N + t + Q * j] = vs[j];
+                    bufW[g * N + t + Q * j] = vw[j];
+                }
             }
         }
         __syncthreads();
@@ -357,6 +367,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const int i2 = args.three_d ? kz : 0;
             const int gm = (G == 2) ? 1 - gg : gg;
             const int kzm = (N - kz) % N;
+            if (!XS(&bufW[gg * N + kz], 427) || !XS(&bufW[gm * N + kzm], 428) || !XS(&outS[gg * N + kz], 429)) continue;
             const cplx<T> xs = bufS[gg * N + kz], xw = bufW[gg * N + kz];
             const cplx<T> ps = bufS[gm * N + kzm], pw = bufW[gm * N + kzm];
             const T h = (T)0.5;
@@ -369,7 +380,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
         __syncthreads();
         if (c == 0 && g < G) {
 #pragma unroll
-            for (int j = 0; j < P; j++) vs[j] = outS[g * N + t + Q * j];
+            for (int j = 0; j < P; j++)
+                if (XS(&outS[g * N + t + Q * j], 430)) vs[j] = outS[g * N + t + Q * j];
         }
     }
     // interior columns: modes j and j + P/2 sit at kz and kz + N/2 and share
@@ -390,8 +402,10 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
                 const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
                 cplx<T> ga, gb;
                 noise_pair_unit<T>(ks, in.seed, i0, i1a, i2a, ga, gb);
-                snoise[j * S::THREADS + tid] = ga;
-                snoise[(j + P / 2) * S::THREADS + tid] = gb;
+                if (XS(&snoise[(j + P / 2) * S::THREADS + tid], 431)) {
+                    snoise[j * S::THREADS + tid] = ga;
+                    snoise[(j + P / 2) * S::THREADS + tid] = gb;
+                }
             }
         }
     }
@@ -419,7 +433,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     reg_fft<T, N, +1>(vs, t, bufS + ln * S::LP, stw);
     if (!valid) return;
 #pragma unroll
-    for (int j = 0; j < P; j++) gS[(long long)(t + Q * j) * args.es] = vs[j];
+    for (int j = 0; j < P; j++)
+        if (XG(&gS[(long long)(t + Q * j) * args.es], 432)) gS[(long long)(t + Q * j) * args.es] = vs[j];
 }
 
 }  // namespace xpfc
