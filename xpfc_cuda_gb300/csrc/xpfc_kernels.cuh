@@ -38,13 +38,19 @@ template <typename T, int L> struct ColShape {
 };
 
 template <typename T, int L, int NG> struct PenShape {
-    // 2*NG [L][TX] tiles (S and W; pencil and, in 3-D, its mirror) near 128 KB
+    // 2*NG [L][TX] tiles (S and W; pencil and, in 3-D, its mirror) near 128 KB;
+    // long 2-D pencils (L >= 256; a 2-D grid has only n0/2 of them) keep
+    // their tiles 32 bytes wide (four FP32 or two FP64 columns) to give the
+    // grid enough blocks; every block stays a whole number of warps
     static constexpr int BYTES = 131072;
-    static constexpr int TXc = BYTES / (2 * NG * L * (int)sizeof(cplx<T>));
+    static constexpr int TXc0 = BYTES / (2 * NG * L * (int)sizeof(cplx<T>));
+    static constexpr int TXc =
+        (NG == 1 && L >= 256 && TXc0 * (int)sizeof(cplx<T>) > 32) ? 32 / (int)sizeof(cplx<T>) : TXc0;
     static constexpr int TX = TXc >= 16 ? 16 : TXc >= 8 ? 8 : TXc >= 4 ? 4 : TXc >= 2 ? 2 : 1;
     static constexpr int TPLc = L >= 32 ? L / 16 : 1;
     static constexpr int TPL = (2 * NG * TX * TPLc > 1024) ? 1024 / (2 * NG * TX) : TPLc;
     static constexpr int THREADS = 2 * NG * TX * TPL;
+    static_assert(THREADS % 32 == 0, "the reductions use full-warp shuffles");
 };
 
 // ---------------------------------------------------------------------------
