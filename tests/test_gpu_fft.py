@@ -7,7 +7,8 @@ pytestmark = pytest.mark.gpu
 
 SHAPES = [(16, 16, 1), (32, 64, 1), (48, 48, 1), (64, 96, 1), (256, 256, 1), (1024, 1024, 1),
           (16, 16, 16), (32, 32, 32), (24, 32, 48), (48, 48, 48), (96, 96, 96), (128, 128, 128),
-          (64, 256, 512), (192, 192, 1), (48, 96, 192), (24, 48, 24), (4096, 64, 1)]
+          (64, 256, 512), (192, 192, 1), (48, 96, 192), (24, 48, 24), (4096, 64, 1), (512, 16, 16),
+          (16, 512, 32), (512, 64, 1)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)

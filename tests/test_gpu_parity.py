@@ -101,7 +101,8 @@ def test_fused_fp64_matches_oracle(oracle_mod, shape, steps):
             assert abs(r["rms"] - rms[i]) <= 1e-8 * abs(rms[i]) + 1e-14, (i, r["rms"], rms[i])
 
 
-@pytest.mark.parametrize("shape,steps", [((4096, 4096, 1), 3), ((2048, 512, 1), 6)])
+@pytest.mark.parametrize("shape,steps", [((4096, 4096, 1), 3), ((2048, 512, 1), 6), ((512, 16, 16), 10),
+                                         ((16, 512, 32), 10)])
 def test_fused_fp64_large_2d_matches_oracle(oracle_mod, shape, steps):
     """Large 2-D FP64 grids, whose pencils are one column wide in shared
     memory (4096) or two (2048)."""
@@ -158,7 +159,8 @@ def test_fused_mixed_within_tolerance(oracle_mod, shape, steps, fcc):
 
 @pytest.mark.parametrize("shape,steps", [((48, 48, 48), 60), ((96, 96, 96), 30), ((192, 192, 1), 60),
                                          ((48, 96, 192), 20), ((512, 512, 1), 30), ((1024, 1024, 1), 20),
-                                         ((256, 2048, 1), 10)])
+                                         ((256, 2048, 1), 10), ((512, 16, 16), 20), ((16, 512, 32), 20),
+                                         ((512, 64, 1), 30)])
 def test_fused_mixed_radix3_sizes(oracle_mod, shape, steps):
     """The 12- and 24-point register plans (48, 96, 192) and the large 2-D
     grids on the mixed path, with conserved noise, against the FP64 oracle."""

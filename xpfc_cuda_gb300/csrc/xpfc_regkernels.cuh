@@ -241,11 +241,17 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int Q = RP<N>::Q, P = RP<N>::P;
     // columns per block: 8 (FP32) for the 16-thread lines; the 4-thread lines
     // of 96 take 16, so that a block still holds four warps
-    static constexpr int TX = (sizeof(T) == 4 ? 8 : 4) * ((Q == 4 && N >= 96) ? 2 : 1);
+    // (the 64-thread lines of the three-level plans take 4, or 2 for FP64
+    // pairs of groups: the slot-0 areas below need LINES x LP >= 2N + G N)
+    static constexpr int TX = RP<N>::three ? ((sizeof(T) == 4 || NG == 1) ? 4 : 2)
+                                           : (sizeof(T) == 4 ? 8 : 4) * ((Q == 4 && N >= 96) ? 2 : 1);
     static constexpr int THREADS = TX * Q * NG;
     static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
     static constexpr int LINES = TX * NG;
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
+    // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
+    // and bufW and writes its results after them in bufW (2N + NG N values)
+    static_assert(!RP<N>::ok || (2 + NG) * N <= LINES * LP, "bufW must hold the slot-0 areas");
     // two resident blocks per SM (128 registers per thread) for the FP32 instances
     static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2 : 1;
 };
