@@ -22,10 +22,15 @@ template <> struct RP<48> { static constexpr bool ok = true, three = false; stat
 template <> struct RP<64> { static constexpr bool ok = true, three = false; static constexpr int P = 8, Q = 8; };
 template <> struct RP<96> { static constexpr bool ok = true, three = false; static constexpr int P = 24, Q = 4; };
 template <> struct RP<192> { static constexpr bool ok = true, three = false; static constexpr int P = 24, Q = 8; };
-// 512 = 8 x 8 x 8: three levels (reg_fft3), 8 values per thread, 64 threads per line
+// 512 = 8 x 8 x 8 and 4096 = 16 x 16 x 16: three levels (reg_fft3), R values
+// per thread, R^2 threads per line
 template <> struct RP<512> {
     static constexpr bool ok = true, three = true;
     static constexpr int P = 8, Q = 64;
+};
+template <> struct RP<4096> {
+    static constexpr bool ok = true, three = true;
+    static constexpr int P = 16, Q = 256;
 };
 template <> struct RP<128> { static constexpr bool ok = true, three = false; static constexpr int P = 16, Q = 8; };
 template <> struct RP<256> { static constexpr bool ok = true, three = false; static constexpr int P = 16, Q = 16; };
@@ -37,7 +42,7 @@ template <> struct RP<256> { static constexpr bool ok = true, three = false; sta
 // for the 32-value plan too, whose 167 registers leave one block per SM and
 // ran slower than the shared-memory kernel (594 against 405 us at 512^3).
 template <typename T, int N> constexpr bool reg_pen_ok() {
-    return RP<N>::ok && (sizeof(T) == 4 ? RP<N>::P <= 24 : RP<N>::P <= 16);
+    return RP<N>::ok && (sizeof(T) == 4 ? RP<N>::P <= 24 : (RP<N>::P <= 16 && RP<N>::Q <= 64));
 }
 template <typename T, int N> constexpr bool reg_line_ok() {
     return RP<N>::ok && RP<N>::P <= 24;

@@ -47,7 +47,10 @@ template <int NQ> struct DSum<float, NQ> {
 // ---------------------------------------------------------------------------
 template <typename T, int N> struct RColShape {
     static constexpr int Q = RP<N>::Q, P = RP<N>::P;
-    static constexpr int TX = sizeof(T) == 4 ? 16 : 8;
+    // 16 (FP32) / 8 (FP64) columns, fewer for long lines (at most 1024 FP32
+    // or 512 FP64 threads, so that the lines stay in registers)
+    static constexpr int TXd = sizeof(T) == 4 ? 16 : 8, MAXT = sizeof(T) == 4 ? 1024 : 512;
+    static constexpr int TX = TXd * Q > MAXT ? MAXT / Q : TXd;
     static constexpr int THREADS = TX * Q;
     static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + (size_t)TX * LP);
@@ -241,17 +244,17 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int Q = RP<N>::Q, P = RP<N>::P;
     // columns per block: 8 (FP32) for the 16-thread lines; the 4-thread lines
     // of 96 take 16, so that a block still holds four warps
-    // (the 64-thread lines of the three-level plans take 4, or 2 for FP64
-    // pairs of groups: the slot-0 areas below need LINES x LP >= 2N + G N)
-    static constexpr int TX = RP<N>::three ? ((sizeof(T) == 4 || NG == 1) ? 4 : 2)
+    // (the three-level plans: 4 columns of 64-thread lines, 2 for FP64 pairs
+    // of groups; 2 columns of the 256-thread lines of 4096)
+    static constexpr int TX = RP<N>::three ? (Q >= 256 ? 2 : (sizeof(T) == 4 || NG == 1) ? 4 : 2)
                                            : (sizeof(T) == 4 ? 8 : 4) * ((Q == 4 && N >= 96) ? 2 : 1);
     static constexpr int THREADS = TX * Q * NG;
     static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
     static constexpr int LINES = TX * NG;
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
     // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
-    // and bufW and writes its results after them in bufW (2N + NG N values)
-    static_assert(!RP<N>::ok || (2 + NG) * N <= LINES * LP, "bufW must hold the slot-0 areas");
+    // and bufW and writes its results after them in bufS (2 NG N values)
+    static_assert(!RP<N>::ok || 2 * NG * N <= LINES * LP, "bufS must hold the slot-0 areas");
     // two resident blocks per SM (128 registers per thread) for the FP32 instances
     static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2 : 1;
 };
@@ -353,7 +356,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     // through shared memory and every thread of the block takes a share,
     // which keeps this rare path small in the instruction stream.
     if (kx0 == 0) {
-        cplx<T> *outS = bufW + 2 * N;                  // after the [group][kz] publish areas
+        cplx<T> *outS = bufS + G * N;                  // after the [group][kz] publish area of S
         __syncthreads();
         if (c == 0 && g < G) {
 #pragma unroll
