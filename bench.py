@@ -16,10 +16,12 @@ rank advances its own independent solve; no collective on the data path).
 --impl reference: the CPU implementation of the same step (the FP64 oracle
 restating the reference's loop, OpenMP on the host cores), rank 0 only.
 
-Two more legs ride on the same line: "sweep" (64 independent solves of
+Three more legs ride on the same line: "sweep" (64 independent solves of
 1000 steps through one xpfc_batch: solves/s, against the same solves one
-context at a time) and "serve" (a Poisson stream of solve requests through
-xpfc_server: latency percentiles and served grid-point-steps/s).
+context at a time), "serve" (a Poisson stream of solve requests through
+xpfc_server: latency percentiles and served grid-point-steps/s) and "two_d"
+(the 2-D step at 4096^2, the reference's own benchmark size, both
+precisions).
 
 Prints one JSON line on rank 0.
 """
@@ -202,6 +204,38 @@ def sweep_cpu_estimate(params, steps, per_size_steps=3):
             "sample": "%d oracle steps per grid size (%s), scaled to %d instances x %d steps" % (
                 per_size_steps, ", ".join("%d^3: %.3f s/step" % (k, v) for k, v in sorted(t_step.items())),
                 len(params), steps)}
+
+
+def run_two_d(args, local, group, barrier):
+    """The 2-D step at the reference's own benchmark size (4096^2, dx = 0.125,
+    single-peak kernel, conserved noise 0.01, diagnostics every 100): device
+    time per step with CUDA events, both precisions."""
+    import torch
+
+    import xpfc_cuda_gb300 as X
+    n = args.two_d_size
+    out = {"grid": "%d^2" % n, "unit": UNIT}
+    for prec, name, k in ((X._lib.MIXED, "mixed", 400), (X._lib.FP64, "fp64", 40)):
+        L = n * DX
+        p = X.default_params(Mx=n, My=n, Mz=1, Lx=L, Ly=L, Lz=1.0, psi0=0.04, sigma=0.25,
+                             peaks=((2 * math.pi, 1.0, 1.0, 8.0),), envelope=X._lib.ENVELOPE_MAX, precision=prec,
+                             t_sample=100, ic_kind=X._lib.IC_NOISE, ic_amp=0.05, noise_amp=0.01, noise_seed=5,
+                             ff_factor=DX ** 2, device=local)
+        stream = torch.cuda.Stream()
+        with X.Xpfc(p, stream=stream.cuda_stream) as x:
+            x.initialize(None)
+            x.step_async(5)
+            x.collect()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            barrier()
+            e0.record(stream)
+            x.step_async(k)
+            e1.record(stream)
+            x.collect()
+            barrier()
+            ms = group.max(e0.elapsed_time(e1))
+        out[name] = {"value": group.sum(n * n * k) / (ms / 1e3) / 1e9, "ms_per_step": ms / k, "steps": k}
+    return out
 
 
 def run_sweep(args, rank, local, group, barrier):
@@ -414,13 +448,17 @@ def run_ours(args):
     if not args.no_serve:
         serve = run_serve(args, rank, local, group, barrier)
 
+    two_d = None
+    if not args.no_two_d:
+        two_d = run_two_d(args, local, group, barrier)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == X._lib.MIXED else "f64",
                 "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, args.precision),
                 "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
-                "fp64": fp64, "sweep": sweep, "serve": serve}
+                "fp64": fp64, "sweep": sweep, "serve": serve, "two_d": two_d}
         print(json.dumps(line), flush=True)
     x.close()
     group.close()
@@ -446,6 +484,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serve-running", type=int, default=16)
+    ap.add_argument("--no-two-d", action="store_true")
+    ap.add_argument("--two-d-size", type=int, default=4096)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

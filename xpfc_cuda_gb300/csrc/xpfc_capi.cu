@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/xpfc.h"
@@ -192,6 +193,50 @@ static const char *kVersion = "xpfc-gb300 0.1 (sm_103a)";
         (ctx)->launches++;       \
         XPFC_CUDA(ctx, call);    \
     } while (0)
+
+// Host loops over whole fields (tens of millions of values) run in 16 fixed
+// chunks on up to 16 threads; the fixed chunking keeps the mean below the
+// same on every machine.
+template <typename F>
+static void par_chunks(size_t n, F fn) {
+    constexpr int K = 16;
+    if (n < ((size_t)1 << 20)) {
+        for (int k = 0; k < K; k++) fn(k, n * k / K, n * (k + 1) / K);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(K);
+    for (int k = 0; k < K; k++) th.emplace_back(fn, k, n * k / K, n * (k + 1) / K);
+    for (auto &t : th) t.join();
+}
+
+// Copies a caller's field and pins its mean to psi0 (Avg_calc.cu:21-43: the
+// difference is added to every value when the mean is not psi0).
+static void stage_and_pin(double *dst, const double *src, size_t n, double psi0) {
+    double part[16] = {0.0};
+    par_chunks(n, [&](int k, size_t b, size_t e) {
+        double s = 0.0;
+        for (size_t i = b; i < e; i++) {
+            dst[i] = src[i];
+            s += src[i];
+        }
+        part[k] = s;
+    });
+    double s = 0.0;
+    for (int k = 0; k < 16; k++) s += part[k];
+    const double m = s / (double)n;
+    const double diff = (m != psi0) ? psi0 - m : 0.0;
+    if (diff != 0.0)
+        par_chunks(n, [&](int, size_t b, size_t e) {
+            for (size_t i = b; i < e; i++) dst[i] += diff;
+        });
+}
+
+static void widen(const float *f, double *d, size_t n) {
+    par_chunks(n, [&](int, size_t b, size_t e) {
+        for (size_t i = b; i < e; i++) d[i] = (double)f[i];
+    });
+}
 
 static int fail(xpfc_ctx *ctx, int code, const std::string &m) {
     if (ctx) ctx->err = m;
@@ -766,8 +811,7 @@ extern "C" int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi) {
         if (rc != XPFC_OK) return rc;
         double *h = (double *)ctx->hstage;
         if (host_psi) {
-            memcpy(h, host_psi, sizeof(double) * n);
-            pin_mean(h, n, ctx->p.psi0);          // configure_avg_density, Avg_calc.cu:21-43
+            stage_and_pin(h, host_psi, n, ctx->p.psi0);   // configure_avg_density, Avg_calc.cu:21-43
         } else {
             rc = build_initial_field(&ctx->p, h);   // the VTK restart
             if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
@@ -1161,8 +1205,7 @@ extern "C" int xpfc_get_field(xpfc_ctx *ctx, double *host_psi) {
     XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->hstage, ctx->X, ctx->esz * n, cudaMemcpyDeviceToHost, ctx->stream));
     XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->esz == 4) {
-        const float *f = (const float *)ctx->hstage;
-        for (size_t i = 0; i < n; i++) host_psi[i] = (double)f[i];
+        widen((const float *)ctx->hstage, host_psi, n);
     } else {
         memcpy(host_psi, ctx->hstage, sizeof(double) * n);
     }
@@ -1450,8 +1493,7 @@ static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) 
     std::vector<char> on_dev(nb, 0);
     for (size_t k = 0; k < nb; k++) {
         if (fields[k]) {
-            memcpy(h + k * n, fields[k], sizeof(double) * n);
-            pin_mean(h + k * n, n, ctx->inst[k].psi0);
+            stage_and_pin(h + k * n, fields[k], n, ctx->inst[k].psi0);
         } else if (ic_on_device(ctx->inst[k])) {
             on_dev[k] = 1;
         } else {
@@ -1569,8 +1611,7 @@ extern "C" int xpfc_batch_get_field(xpfc_batch *b, int i, double *host_psi) {
     XPFC_CUDA(b, cudaMemcpyAsync(ctx->hstage, ctx->X, ctx->esz * n, cudaMemcpyDeviceToHost, ctx->stream));
     XPFC_CUDA(b, cudaStreamSynchronize(ctx->stream));
     if (ctx->esz == 4) {
-        const float *f = (const float *)ctx->hstage;
-        for (size_t j = 0; j < n; j++) host_psi[j] = (double)f[j];
+        widen((const float *)ctx->hstage, host_psi, n);
     } else {
         memcpy(host_psi, ctx->hstage, sizeof(double) * n);
     }
