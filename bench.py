@@ -45,7 +45,7 @@ FCC = ((2 * math.pi, 1.0, 1.0, 8.0), (2 * math.pi * 2 / math.sqrt(3), 1.0, 1.0, 
 # per-pass algorithmic bytes as multiples of one packed field array (N^3 elements)
 PASS_NAMES = {0: "pencil_kernel", 1: "col_kernel(inverse)", 2: "row_kernel(fused)", 3: "col_kernel(forward)"}
 PASS_ARRAYS = {0: 3, 1: 2, 2: 2, 3: 2}
-SURVEY_BYTES_PER_POINT = 16.125   # two read+write sweeps of the FP32 state at 256^3
+FLOOR_BYTES_PER_POINT = 16.125   # two read+write sweeps of the FP32 state at 256^3
 SIGMA = 0.22
 
 
@@ -433,7 +433,7 @@ def run_ours(args):
                 "passes": {PASS_NAMES[k]: {"avg_ms": v[0] / v[1], "launches": v[1],
                                            "GB/s": PASS_ARRAYS[k] * esz * n ** 3 / (v[0] / v[1] / 1e3) / 1e9}
                            for k, v in passes.items()},
-                "step_frac_of_two_sweep_floor": (value * 1e9 / ws) * SURVEY_BYTES_PER_POINT / (peak * 1e9)}
+                "step_frac_of_two_sweep_floor": (value * 1e9 / ws) * FLOOR_BYTES_PER_POINT / (peak * 1e9)}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
