@@ -80,6 +80,14 @@ __device__ __forceinline__ void pdl_wait() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// The same pointer, with its value hidden from the compiler: addresses (and
+// shared-memory loads) derived from it are recomputed at the new use instead
+// of being kept in registers from an earlier use of the same expressions.
+template <typename P> __device__ __forceinline__ P *opaque(P *p) {
+    asm volatile("" : "+l"(p));
+    return p;
+}
+
 // Batched launches: grid z indexes the instance; instance z's field starts
 // z * zstride complex elements after the base pointers and its partial sums
 // follow the other instances' (block_slot).  One field: zstride = 0, nz = 1.

@@ -255,8 +255,11 @@ template <typename T, int N, int NG> struct RPenShape {
     // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
     // and bufW and writes its results after them in bufS (2 NG N values)
     static_assert(!RP<N>::ok || 2 * NG * N <= LINES * LP, "bufS must hold the slot-0 areas");
-    // two resident blocks per SM (128 registers per thread) for the FP32 instances
-    static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2 : 1;
+    // two resident blocks per SM (128 registers per thread) for the FP32
+    // instances of 256 threads; three (168 registers) for the 24-value lines
+    static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2
+                                : (sizeof(T) == 4 && P > 16)                  ? 3
+                                                                              : 1;
 };
 
 // k-space sums of one updated mode: weight c2 |X|^2 (free energy) and
@@ -335,16 +338,38 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     const long long off = (long long)blockIdx.z * args.zstride + (long long)yg * args.gstride + kx0 + c;
     cplx<T> *gS = reinterpret_cast<cplx<T> *>(args.S) + off;
     const cplx<T> *gW = reinterpret_cast<const cplx<T> *>(args.W) + off;
+    // Plans of 24 values per thread would hold 48 values of S and W through
+    // both transforms (over 255 registers, with spills).  They load and
+    // transform W first and keep it in its line's scratch of bufW, in natural
+    // order (element kz at ln LP + kz), until the update; S is loaded and
+    // transformed after.
+    constexpr bool STASH = P > 16;
+    // distance between the two groups' kx = 0 pencils of W in bufW
+    constexpr int WG = STASH ? TX * S::LP : N;
     cplx<T> vs[P], vw[P];
 #pragma unroll
     for (int j = 0; j < P; j++) {
         const long long e = (long long)(t + Q * j) * args.es;
-        vs[j] = (valid && XG(&gS[e], 423)) ? gS[e] : mk<T>((T)0, (T)0);
+        if constexpr (!STASH) vs[j] = (valid && XG(&gS[e], 423)) ? gS[e] : mk<T>((T)0, (T)0);
         vw[j] = (valid && XG(&gW[e], 424)) ? gW[e] : mk<T>((T)0, (T)0);
     }
     __syncthreads();
     const int ln = g * TX + c;
-    reg_fft2<T, N, -1>(vs, vw, t, bufS + ln * S::LP, bufW + ln * S::LP, stw);
+    if constexpr (STASH) {
+        reg_fft<T, N, -1>(vw, t, bufW + ln * S::LP, stw);
+        __syncthreads();   // every thread of the line is done reading its scratch
+#pragma unroll
+        for (int j = 0; j < P; j++)
+            if (XS(&bufW[ln * S::LP + t + Q * j], 433)) bufW[ln * S::LP + t + Q * j] = vw[j];
+#pragma unroll
+        for (int j = 0; j < P; j++) {
+            const long long e = (long long)(t + Q * j) * args.es;
+            vs[j] = (valid && XG(&gS[e], 423)) ? gS[e] : mk<T>((T)0, (T)0);
+        }
+        reg_fft<T, N, -1>(vs, t, bufS + ln * S::LP, stw);
+    } else {
+        reg_fft2<T, N, -1>(vs, vw, t, bufS + ln * S::LP, bufW + ln * S::LP, stw);
+    }
 
     DSum<T, NQ_PEN> acc;
     const T sc = (T)args.scale;
@@ -354,17 +379,19 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     // slot 0 (only in the block holding kx' = 0): the kx = 0 and kx = n0/2
     // planes separate with the mirror mode (-k1, -k2).  Those pencils go
     // through shared memory and every thread of the block takes a share,
-    // which keeps this rare path small in the instruction stream.
+    // which keeps this rare path small in the instruction stream.  The
+    // pencils of S are published as [group][kz] at the start of bufS; those
+    // of W as [group][kz] at the start of bufW, or where the stash already
+    // holds them (group gg at gg WG).
     if (kx0 == 0) {
         cplx<T> *outS = bufS + G * N;                  // after the [group][kz] publish area of S
         __syncthreads();
         if (c == 0 && g < G) {
 #pragma unroll
             for (int j = 0; j < P; j++) {
-                if (XS(&bufS[g * N + t + Q * j], 425) && XS(&bufW[g * N + t + Q * j], 426)) {
-                    bufS[g * N + t + Q * j] = vs[j];
-                    bufW[g * N + t + Q * j] = vw[j];
-                }
+                if (XS(&bufS[g * N + t + Q * j], 425)) bufS[g * N + t + Q * j] = vs[j];
+                if constexpr (!STASH)
+                    if (XS(&bufW[g * N + t + Q * j], 426)) bufW[g * N + t + Q * j] = vw[j];
             }
         }
         __syncthreads();
@@ -376,9 +403,9 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const int i2 = args.three_d ? kz : 0;
             const int gm = (G == 2) ? 1 - gg : gg;
             const int kzm = (N - kz) % N;
-            if (!XS(&bufW[gg * N + kz], 427) || !XS(&bufW[gm * N + kzm], 428) || !XS(&outS[gg * N + kz], 429)) continue;
-            const cplx<T> xs = bufS[gg * N + kz], xw = bufW[gg * N + kz];
-            const cplx<T> ps = bufS[gm * N + kzm], pw = bufW[gm * N + kzm];
+            if (!XS(&bufW[gg * WG + kz], 427) || !XS(&bufW[gm * WG + kzm], 428) || !XS(&outS[gg * N + kz], 429)) continue;
+            const cplx<T> xs = bufS[gg * N + kz], xw = bufW[gg * WG + kz];
+            const cplx<T> ps = bufS[gm * N + kzm], pw = bufW[gm * WG + kzm];
             const T h = (T)0.5;
             const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
             const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
@@ -430,8 +457,13 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
                 na = cscale(snoise[j * S::THREADS + tid], noise_amp_of<T>(ks, ca.k2));
                 nb = cscale(snoise[(j + P / 2) * S::THREADS + tid], noise_amp_of<T>(ks, cb.k2));
             }
-            vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, (T)2), sc);
-            vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, (T)2), sc);
+            cplx<T> wa = vw[j], wb = vw[j + P / 2];
+            if constexpr (STASH) {
+                wa = XS(&bufW[ln * S::LP + kza], 434) ? bufW[ln * S::LP + kza] : zero;
+                wb = XS(&bufW[ln * S::LP + kzb], 435) ? bufW[ln * S::LP + kzb] : zero;
+            }
+            vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], wa, na, acc, (T)2), sc);
+            vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], wb, nb, acc, (T)2), sc);
         }
     }
     if (RED) {
@@ -439,11 +471,17 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
         block_reduce_store<NQ_PEN>(tot, args.partials + block_slot() * NQ_PEN, sred);
     }
     if (!args.update) return;
-    reg_fft<T, N, +1>(vs, t, bufS + ln * S::LP, stw);
+    // The twiddles and the global addresses are taken afresh from opaque
+    // copies of their base pointers: otherwise the compiler keeps the forward
+    // transform's twiddles and the loads' addresses in registers through the
+    // whole update (158 instead of 194 registers at N = 128).
+    reg_fft<T, N, +1>(vs, t, bufS + ln * S::LP, opaque(stw));
     if (!valid) return;
+    cplx<T> *o = opaque(gS) + (long long)t * args.es;
+    const long long step = (long long)Q * args.es;
 #pragma unroll
-    for (int j = 0; j < P; j++)
-        if (XG(&gS[(long long)(t + Q * j) * args.es], 432)) gS[(long long)(t + Q * j) * args.es] = vs[j];
+    for (int j = 0; j < P; j++, o += step)
+        if (XG(o, 432)) *o = vs[j];
 }
 
 }  // namespace xpfc
