@@ -61,7 +61,15 @@ def test_server_results_equal_single_runs():
         assert st["done"] == len(mix) and st["failed"] == 0
     for k, ((p, n), (f, recs)) in enumerate(zip(mix, got)):
         f1, r1 = _alone(X, p, n, given if k == 2 else None)
-        assert np.array_equal(f, f1), k
+        if not np.array_equal(f, f1):
+            # say which side moved: a second solve alone, and where they differ
+            f2, _ = _alone(X, p, n, given if k == 2 else None)
+            d = np.abs(f - f1).reshape(-1)
+            idx = np.flatnonzero(d)
+            pytest.fail("request %d: %d of %d values differ (max %.3e, first %s); non-finite: served %d, alone %d; "
+                        "a second solve alone equals the first: %s, equals the served one: %s" % (
+                            k, idx.size, d.size, float(np.nanmax(d)), idx[:4].tolist(), int((~np.isfinite(f)).sum()),
+                            int((~np.isfinite(f1)).sum()), bool(np.array_equal(f1, f2)), bool(np.array_equal(f, f2))))
         assert recs == r1, k
 
 

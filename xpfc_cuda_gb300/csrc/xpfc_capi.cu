@@ -232,6 +232,18 @@ static void stage_and_pin(double *dst, const double *src, size_t n, double psi0)
         });
 }
 
+// Diagnostics switch XPFC_POISON=1: every state buffer is filled with
+// all-one bytes (a NaN in FP32 and in FP64) when it is allocated, so that a
+// kernel reading an element that nothing wrote makes the results non-finite
+// instead of depending on what the allocator handed back.
+static void poison(void *p, size_t bytes, cudaStream_t s) {
+    static const bool on = [] {
+        const char *e = getenv("XPFC_POISON");
+        return e && e[0] == '1';
+    }();
+    if (on && p) cudaMemsetAsync(p, 0xFF, bytes, s);
+}
+
 static void widen(const float *f, double *d, size_t n) {
     par_chunks(n, [&](int, size_t b, size_t e) {
         for (size_t i = b; i < e; i++) d[i] = (double)f[i];
@@ -449,6 +461,7 @@ static int ensure_partials(xpfc_ctx *ctx, size_t n) {
     if (ctx->partials) cudaFree(ctx->partials);
     ctx->partials = nullptr;
     XPFC_CUDA(ctx, cudaMalloc(&ctx->partials, sizeof(double) * n));
+    poison(ctx->partials, sizeof(double) * n, ctx->stream);
     ctx->partials_cap = n;
     return XPFC_OK;
 }
@@ -521,6 +534,8 @@ static int create_group(const xpfc_params *ps, int nb, xpfc_ctx **out) {
         xpfc_destroy(ctx);
         return XPFC_ENOMEM;
     }
+    poison(ctx->S, bytes, ctx->stream);
+    poison(ctx->W, bytes, ctx->stream);
     rc = build_tables(ctx);
     if (rc == XPFC_OK) {
         const int L0 = ctx->L0;
@@ -1167,7 +1182,10 @@ template <typename T>
 static int field_to_X(xpfc_ctx *ctx, int k = 0) {
     const bool dbl = sizeof(T) == 8;
     void *Sk = (char *)ctx->S + ctx->esz * (size_t)ctx->ncells * k;
-    if (!ctx->X) XPFC_CUDA(ctx, cudaMalloc(&ctx->X, ctx->esz * (size_t)ctx->ncells));
+    if (!ctx->X) {
+        XPFC_CUDA(ctx, cudaMalloc(&ctx->X, ctx->esz * (size_t)ctx->ncells));
+        poison(ctx->X, ctx->esz * (size_t)ctx->ncells, ctx->stream);
+    }
     void *tw0 = twiddle(ctx, ctx->L0, dbl), *tw2 = twiddle(ctx, ctx->n0, dbl);
     if (!tw0 || !tw2) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
     RowArgs ra{};
