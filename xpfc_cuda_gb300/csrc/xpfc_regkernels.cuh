@@ -346,6 +346,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     constexpr bool STASH = P > 16;
     // distance between the two groups' kx = 0 pencils of W in bufW
     constexpr int WG = STASH ? TX * S::LP : N;
+    static_assert(!STASH || (N <= S::LP && (NG - 1) * WG + N <= S::LINES * S::LP),
+                  "a line's scratch must hold its parked W pencil");
     cplx<T> vs[P], vw[P];
 #pragma unroll
     for (int j = 0; j < P; j++) {
