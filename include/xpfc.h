@@ -290,16 +290,18 @@ int xpfc_server_stats_get(xpfc_server *s, xpfc_server_stats *st);
 /* No counterpart in the reference.  The free energy of xpfc_FE_calc
    (ff_factor times the sum of the FE_calc density) from five caller-owned
    device arrays of n doubles, for callers that cannot allocate device memory
-   (inside a stream capture that must not grow a memory pool, or under a host
-   framework that owns all device memory).  Allocates nothing: its partial sums
-   live in a fixed 32 KB array in the library's device memory, which every GPU
-   that loads the library keeps until exit.  n is at most
-   XPFC_NOALLOC_MAX_POINTS (2^28; larger n returns XPFC_EINVAL).  stream is a
-   cudaStream_t (NULL: the legacy default stream); the call waits for its own
-   work and writes *F on the host.  The first call on each device looks up the
-   array's device address (cudaGetSymbolAddress) and must come before any
-   stream capture.  All calls share the array: calls that overlap on the GPU
-   race, so serialise them. */
+   (a host framework that owns all device memory through its own pool and
+   forbids plugins to allocate, or a loop run under a fixed device-memory
+   budget).  Allocates nothing: its partial sums live in a fixed 32 KB array
+   in the library's device memory, which every GPU that loads the library
+   keeps until exit.  n is at most XPFC_NOALLOC_MAX_POINTS (2^28; larger n
+   returns XPFC_EINVAL).  stream is a cudaStream_t (NULL: the legacy default
+   stream); the call waits for its own work on that stream and writes *F on
+   the host.  The first call on each device looks up the array's device
+   address (cudaGetSymbolAddress) and must come before any stream capture;
+   the address is kept for the process, so cudaDeviceReset after that first
+   call is not supported.  All calls share the array: calls that overlap on
+   the GPU race, so serialise them. */
 #define XPFC_NOALLOC_CHUNK 65536
 #define XPFC_NOALLOC_MAX_CHUNKS 4096
 #define XPFC_NOALLOC_MAX_POINTS ((long long)XPFC_NOALLOC_CHUNK * XPFC_NOALLOC_MAX_CHUNKS)

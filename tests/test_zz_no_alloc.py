@@ -46,11 +46,20 @@ def test_fe_noalloc_matches_fe_calc_twice():
 
 
 def test_fe_noalloc_rejects_oversize_and_null():
+    """Sizes beyond the fixed scratch and null arrays are refused before any
+    launch (the arrays here are real, small device buffers)."""
+    import torch
+
     import xpfc_cuda_gb300 as X
     L = X.load()
     F = C.c_double()
-    one = C.c_void_p(16)   # never dereferenced: the size check comes first
+    small = torch.zeros(16, dtype=torch.float64, device="cuda")
+    one = C.c_void_p(small.data_ptr())
     rc = L.xpfc_FE_calc_noalloc(one, one, one, one, one, (1 << 28) + 1, 1.0, 1.0, 1.0, C.byref(F), None)
     assert rc == X._lib.EINVAL and b"exceed the maximum" in L.xpfc_last_error(None)
     rc = L.xpfc_FE_calc_noalloc(None, one, one, one, one, 10, 1.0, 1.0, 1.0, C.byref(F), None)
     assert rc == X._lib.EINVAL
+    # a valid call on the same buffers still works: 16 zeros sum to zero
+    rc = L.xpfc_FE_calc_noalloc(one, one, one, one, one, 16, 1.0, 1.0, 1.0, C.byref(F),
+                                torch.cuda.current_stream().cuda_stream)
+    assert rc == X._lib.OK and F.value == 0.0

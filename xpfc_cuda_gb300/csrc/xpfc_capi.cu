@@ -100,8 +100,16 @@ struct xpfc_ctx {
     // fused state (T = float for XPFC_MIXED, double for XPFC_FP64)
     void *S = nullptr, *W = nullptr, *X = nullptr;
     size_t esz = 8;
-    // twiddle tables W_L^k (k < L), keyed by (L, is_double)
+    // twiddle tables W_L^k (k < L), keyed by (L, is_double), and the host
+    // sources of their stream-ordered uploads
     std::map<long long, void *> tw;
+    std::map<long long, std::vector<unsigned char>> tw_host;
+    // host sources of the stream-ordered uploads of the coefficient tables
+    // and of the batch arrays (kept until the next upload or destroy)
+    std::vector<double> table_host_d;
+    std::vector<float> table_host_f;
+    std::vector<double> pin_host;
+    std::vector<unsigned long long> seed_host;
     // per-shell coefficient tables
     void *table_f = nullptr, *table_d = nullptr;
     int mmax = 0;
@@ -345,25 +353,36 @@ static double c2_of(const xpfc_params &p, double kmag) {
     return acc;
 }
 
+// Twiddle table W_L^k of one length and precision, built on first use.  The
+// upload is ordered on the context's stream (every launch that reads the
+// table comes after it on that stream, or on an auxiliary stream forked from
+// it later), and its host source stays alive in the context until destroy,
+// so no kernel can read a partly written table.
 static void *twiddle(xpfc_ctx *ctx, int L, bool dbl) {
     const long long key = 2LL * L + (dbl ? 1 : 0);
     auto it = ctx->tw.find(key);
     if (it != ctx->tw.end()) return it->second;
-    std::vector<double> h(2 * (size_t)L);
+    const size_t bytes = (dbl ? sizeof(double) : sizeof(float)) * 2 * (size_t)L;
+    std::vector<unsigned char> &h = ctx->tw_host[key];
+    h.resize(bytes);
     for (int k = 0; k < L; k++) {
         const double ang = 2.0 * M_PI * (double)k / (double)L;
-        h[2 * k] = std::cos(ang);
-        h[2 * k + 1] = -std::sin(ang);
+        const double c = std::cos(ang), s = -std::sin(ang);
+        if (dbl) {
+            reinterpret_cast<double *>(h.data())[2 * k] = c;
+            reinterpret_cast<double *>(h.data())[2 * k + 1] = s;
+        } else {
+            reinterpret_cast<float *>(h.data())[2 * k] = (float)c;
+            reinterpret_cast<float *>(h.data())[2 * k + 1] = (float)s;
+        }
     }
     void *d = nullptr;
-    if (dbl) {
-        if (cudaMalloc(&d, sizeof(double) * 2 * L) != cudaSuccess) return nullptr;
-        cudaMemcpy(d, h.data(), sizeof(double) * 2 * L, cudaMemcpyHostToDevice);
-    } else {
-        std::vector<float> f(2 * (size_t)L);
-        for (size_t i = 0; i < f.size(); i++) f[i] = (float)h[i];
-        if (cudaMalloc(&d, sizeof(float) * 2 * L) != cudaSuccess) return nullptr;
-        cudaMemcpy(d, f.data(), sizeof(float) * 2 * L, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMalloc(&d, bytes);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, h.data(), bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) {
+        if (d) cudaFree(d);
+        ctx->err = std::string("twiddle table upload: ") + cudaGetErrorString(e);
+        return nullptr;
     }
     ctx->tw[key] = d;
     return d;
@@ -428,8 +447,13 @@ static int build_tables(xpfc_ctx *ctx) {
     const int h0 = ctx->n0 / 2, h1 = ctx->n1 / 2, h2 = ctx->n2 / 2;
     ctx->mmax = h0 * h0 + h1 * h1 + h2 * h2;
     const size_t nm = (size_t)ctx->mmax + 1;
-    std::vector<double> td(4 * nm * ctx->nb);
-    std::vector<float> tf(4 * nm * ctx->nb);
+    // the host sources of the last upload stay alive in the context; a new
+    // upload (a pooled context taking new params) waits for the last one
+    if (!ctx->table_host_d.empty()) XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<double> &td = ctx->table_host_d;
+    std::vector<float> &tf = ctx->table_host_f;
+    td.assign(4 * nm * ctx->nb, 0.0);
+    tf.assign(4 * nm * ctx->nb, 0.f);
     const double dk = 2.0 * M_PI / ctx->Lax[0];
     for (int i = 0; i < ctx->nb; i++) {
         const xpfc_params &p = ctx->inst[i];
@@ -448,7 +472,7 @@ static int build_tables(xpfc_ctx *ctx) {
     // the size depends only on the grid and nb, so a reused context keeps its buffers
     if (!ctx->table_d) XPFC_CUDA(ctx, cudaMalloc(&ctx->table_d, sizeof(double) * td.size()));
     if (!ctx->table_f) XPFC_CUDA(ctx, cudaMalloc(&ctx->table_f, sizeof(float) * tf.size()));
-    // pageable sources: each call returns once its source is staged
+    // stream-ordered: every pass that reads the tables comes after these
     XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->table_d, td.data(), sizeof(double) * td.size(), cudaMemcpyHostToDevice,
                                    ctx->stream));
     XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->table_f, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice,
@@ -474,6 +498,8 @@ static int check_params(const xpfc_params *q) {
     if (q->dt <= 0.0 || q->npeaks < 1 || q->npeaks > XPFC_MAX_PEAKS)
         return fail(nullptr, XPFC_EINVAL, "dt must be > 0 and 1 <= npeaks <= 8");
     if (q->precision != XPFC_FP64 && q->precision != XPFC_MIXED) return fail(nullptr, XPFC_EINVAL, "bad precision");
+    if (q->device < 0 || q->device >= 64)
+        return fail(nullptr, XPFC_EINVAL, "device ordinal must be in [0, 64) (per-device launch set-up flags)");
     const bool three = q->Mz > 1;
     const int n0 = three ? q->Mz : q->My, n1 = three ? q->My : q->Mx, n2 = three ? q->Mx : 1;
     if (n0 % 2 != 0 || n1 % 2 != 0 || (three && n2 % 2 != 0))
@@ -549,17 +575,30 @@ static int create_group(const xpfc_params *ps, int nb, xpfc_ctx **out) {
     }
     if (rc == XPFC_OK && cudaMalloc(&ctx->init_red, sizeof(double) * 8 * nb) != cudaSuccess) rc = XPFC_ENOMEM;
     if (rc == XPFC_OK && nb > 1) {
-        std::vector<double> pv(nb);
-        std::vector<unsigned long long> sd(nb);
+        // per-instance pinned means and noise seeds, uploaded on the context's
+        // stream (ordered before every pass) from host copies the context keeps
+        std::vector<double> &pv = ctx->pin_host;
+        std::vector<unsigned long long> &sd = ctx->seed_host;
+        pv.resize(nb);
+        sd.resize(nb);
         for (int i = 0; i < nb; i++) {
             pv[i] = ps[i].psi0 * (double)ctx->ncells;
             sd[i] = ps[i].noise_seed;
         }
         if (cudaMalloc(&ctx->pin_values, sizeof(double) * nb) != cudaSuccess ||
-            cudaMalloc(&ctx->seeds, sizeof(unsigned long long) * nb) != cudaSuccess ||
-            cudaMemcpy(ctx->pin_values, pv.data(), sizeof(double) * nb, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(ctx->seeds, sd.data(), sizeof(unsigned long long) * nb, cudaMemcpyHostToDevice) != cudaSuccess)
+            cudaMalloc(&ctx->seeds, sizeof(unsigned long long) * nb) != cudaSuccess) {
             rc = XPFC_ENOMEM;
+        } else {
+            cudaError_t e2 = cudaMemcpyAsync(ctx->pin_values, pv.data(), sizeof(double) * nb,
+                                             cudaMemcpyHostToDevice, ctx->stream);
+            if (e2 == cudaSuccess)
+                e2 = cudaMemcpyAsync(ctx->seeds, sd.data(), sizeof(unsigned long long) * nb,
+                                     cudaMemcpyHostToDevice, ctx->stream);
+            if (e2 != cudaSuccess) {
+                ctx->err = std::string("batch array upload: ") + cudaGetErrorString(e2);
+                rc = XPFC_ECUDA;
+            }
+        }
     }
     if (rc != XPFC_OK) {
         set_thread_error(ctx->err.empty() ? "context set-up failed" : ctx->err);

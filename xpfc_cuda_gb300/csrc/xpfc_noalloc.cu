@@ -2,12 +2,12 @@
 // allocation, for callers that cannot call cudaMalloc.
 //
 // Who needs it: code that runs where the CUDA allocator is off limits, e.g.
-// inside a stream capture that must not grow a memory pool, under a host
-// framework that owns all device memory and forbids allocations from plugins,
-// or in a hot loop that budgets out every allocation.  xpfc_FE_calc reduces
-// through a context-owned buffer that xpfc_create allocated; this variant
-// takes the five density arrays from the caller and keeps its partial sums in
-// a fixed array in the library's own device memory.
+// a host framework that owns all device memory through its own pool and
+// forbids plugins to allocate behind its back, or a solver loop run under a
+// fixed device-memory budget that counts every allocation.  xpfc_FE_calc
+// reduces through a context-owned buffer that xpfc_create allocated; this
+// variant takes the five density arrays from the caller and keeps its partial
+// sums in a fixed array in the library's own device memory.
 //
 // The scratch: g_fe_scratch, a file-scope __device__ array of
 // XPFC_NOALLOC_MAX_CHUNKS + 1 doubles (32 KB).  Every GPU that loads the
@@ -17,12 +17,16 @@
 // larger fields are rejected with XPFC_EINVAL.  Every call shares the array
 // and overwrites the slots it uses (the result slot is cleared first), so two
 // calls whose kernels overlap on the GPU race: serialise them (one stream, or
-// events).
+// events).  The call waits for its own work on the given stream and returns
+// F on the host.
 //
 // Host code must not hand the array's name to a kernel: on the host the name
 // is only a stand-in for the device symbol.  The device address is looked up
 // once per device with cudaGetSymbolAddress, on the first call made while
 // that device is current; make that first call before any stream capture.
+// The address is kept for the life of the process, so a cudaDeviceReset
+// after the first call (which reloads the library's module and may move the
+// array) is not supported.
 #include <cuda_runtime.h>
 
 #include <mutex>
