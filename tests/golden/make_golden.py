@@ -66,8 +66,11 @@ def parse_kv(path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("XPFC_REFERENCE", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("XPFC_REFERENCE"),
+                    help="the reference tree (or XPFC_REFERENCE)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref or set XPFC_REFERENCE")
     subprocess.run(["make", "-s", "-C", REFDIR, f"REF={args.ref}"], check=True)
     for name, text, vtk_in, keep_vtk in cases():
         with tempfile.TemporaryDirectory() as d:

@@ -1,0 +1,129 @@
+"""Generate golden vectors from LC2500/XPFC_CUDA's own program run on a GPU.
+
+Runs on the GPU machine.  Builds the reference program from its staged sources
+(baseline/ref_gpu.py: the reference's own CUDA code for sm_103a, cuFFT for its
+transforms; the output-precision build prints F and the residual with 17
+digits and writes the VTK field with 17 digits) and runs it on the decks of
+make_golden.py plus two 512^2 decks (the 64^3-point 2-D analogue: dx = 0.125,
+a seeded noise liquid read through the iconfig = 10 restart, 61 and 2001
+loop iterations).  Each deck gives tests/golden/gpu_<name>.npz with the
+full-precision F and residual series and final field, the same series from the
+unmodified-output build, and the run's metadata.  Also probes the build linked
+against cuFFT as shipped (whose cufftXtSetGPUs is given one GPU) and times the
+reference loop (its TIMING line, main.cu:305,437) at 512^2 and 4096^2.
+
+Usage (GPU machine, sources staged):
+    python tests/golden/make_golden_gpu.py [--out DIR] [--no-timing]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, HERE)
+
+from baseline import ref_gpu  # noqa: E402
+from make_golden import cases, deck, vtk_text  # noqa: E402
+
+
+def gpu_cases():
+    rng = np.random.default_rng(20261204)
+    noise512 = 0.05 + 0.1 * rng.standard_normal(512 * 512)
+    out = [(name, text, vtk_in) for name, text, vtk_in, _ in cases()]
+    out.append(("noise512_t60", deck(0.05, 0.2, 1, 3, 0, 1, 64, 64, 512, 512, 60, 1, 20, 10), noise512))
+    out.append(("noise512_t2000", deck(0.05, 0.2, 1, 3, 0, 1, 64, 64, 512, 512, 2000, 1, 100, 10), noise512))
+    return out
+
+
+def t_sample_of(text):
+    return int(text.split("\n")[9].split()[0])
+
+
+def dims_of(vtk_in):
+    return int(round(np.sqrt(vtk_in.size)))
+
+
+def meta():
+    m = {}
+    try:
+        m["gpu"] = subprocess.run(["nvidia-smi", "--query-gpu=name,driver_version", "--format=csv,noheader"],
+                                  capture_output=True, text=True).stdout.strip()
+    except OSError:
+        m["gpu"] = None
+    try:
+        m["nvcc"] = subprocess.run([ref_gpu._nvcc(), "--version"], capture_output=True, text=True).stdout.strip()
+    except OSError:
+        m["nvcc"] = None
+    try:
+        with open(os.path.join(ref_gpu.BIN, "BUILD.json")) as f:
+            m["build"] = json.load(f)
+    except OSError:
+        m["build"] = None
+    return m
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=HERE)
+    ap.add_argument("--no-timing", action="store_true")
+    a = ap.parse_args()
+    os.makedirs(a.out, exist_ok=True)
+    progs = ref_gpu.build()
+    info = meta()
+
+    # the program linked against cuFFT as shipped, on the smallest deck
+    name, text, vtk_in = gpu_cases()[2]
+    stock = ref_gpu.run(progs["xpfc_ref_stock"], text, t_sample_of(text), keep_field=False, timeout=300)
+    lines = [ln for ln in (stock["stdout_tail"] + stock["stderr_tail"]).splitlines() if "cufftXtSetGpus" in ln]
+    info["stock_cufft_xt_one_gpu"] = {"deck": name, "returncode": stock["returncode"], "lines": lines}
+    print("stock build:", info["stock_cufft_xt_one_gpu"], flush=True)
+
+    for name, text, vtk_in in gpu_cases():
+        ts = t_sample_of(text)
+        vtk = vtk_text(vtk_in, dims_of(vtk_in), dims_of(vtk_in), 0.125) if vtk_in is not None else None
+        hp = ref_gpu.run(progs["xpfc_ref_hp"], text, ts, vtk_in=vtk, timeout=900)
+        lo = ref_gpu.run(progs["xpfc_ref"], text, ts, vtk_in=vtk, keep_field=False, timeout=900)
+        if hp["returncode"] != 0 or lo["returncode"] != 0 or "psi_final" not in hp:
+            print(name, "FAILED", hp["returncode"], lo["returncode"], hp["stdout_tail"][-1500:],
+                  hp["stderr_tail"][-1500:], flush=True)
+            continue
+        extra = {"vtk_in": vtk_in} if vtk_in is not None else {}
+        np.savez_compressed(
+            os.path.join(a.out, "gpu_%s.npz" % name),
+            deck=np.frombuffer(text.encode(), dtype=np.uint8),
+            F=np.array(hp["F"], dtype=np.float64).reshape(-1, 2),
+            RMS=np.array(hp["RMS"], dtype=np.float64).reshape(-1, 2),
+            psi_final=hp["psi_final"],
+            final_iteration=np.array([hp["final_iteration"]]),
+            F_stock_output=np.array(lo["F"], dtype=np.float64).reshape(-1, 2),
+            RMS_stock_output=np.array(lo["RMS"], dtype=np.float64).reshape(-1, 2),
+            meta=np.frombuffer(json.dumps(dict(info, timing=hp["timing"])).encode(), dtype=np.uint8),
+            **extra)
+        print(name, "F", hp["F"][:2], "...", hp["F"][-1:], "RMS", hp["RMS"][:1], "timing", hp["timing"], flush=True)
+
+    if not a.no_timing:
+        timing = {"meta": info, "runs": []}
+        for M, t, dt in ((512, 100, 1.0), (4096, 25, 0.25)):
+            for ts in (1000000, 100):
+                text = deck(0.05, 0.25, 1, 3, 0.1, 1, M // 8, M // 8, M, M, t, dt, ts, 0, iseed=1, ishape=1,
+                            h=4.0, k=4.0, roa=6.0)
+                r = ref_gpu.run(progs["xpfc_ref"], text, ts, keep_field=False, timeout=900)
+                steps = int(t / dt + 1)
+                ms = r["timing"].get("Full iteration time.")
+                rec = {"grid": "%d^2" % M, "loop_iterations": steps, "t_sample": ts, "loop_ms": ms,
+                       "returncode": r["returncode"],
+                       "gpt_steps_per_s": (M * M * steps / (ms / 1e3) / 1e9) if ms else None}
+                timing["runs"].append(rec)
+                print("timing", rec, flush=True)
+        with open(os.path.join(a.out, "reference_gpu_timing.json"), "w") as f:
+            json.dump(timing, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
