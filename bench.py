@@ -132,9 +132,65 @@ def cpu_baseline(n, steps=None, target_s=15.0):
         t1, _ = O.bench(p, psi, 1)
         steps = max(1, min(40, int(target_s / max(t1, 1e-3))))
     sec, _ = O.bench(p, psi, steps)
-    return {"value": n ** 3 * steps / sec / 1e9, "unit": UNIT, "cores": O.threads(), "kind": "port",
+    return {"value": n ** 3 * steps / sec / 1e9, "unit": UNIT, "cores": O.threads(), "host_cpus": os.cpu_count(),
+            "kind": "port",
             "sample": "%d full steps of the %d^3 workload (FP64 oracle, OpenMP, %d threads), %.1f s" % (
                 steps, n, O.threads(), sec)}
+
+
+def accuracy(X, n, rank, local, host_psi, k):
+    """The mixed-precision step against the FP64 oracle on the benchmark's own
+    workload: k steps of the n^3 case from the same initial field (the oracle
+    runs them on the host cores), free energy and field compared."""
+    import numpy as np
+    from oracle import oracle as O
+    L = n * DX
+    q = workload_params(X, n, X._lib.MIXED, rank)
+    q.device = local
+    q.t_sample = k
+    with X.Xpfc(q) as x:
+        x.initialize(host_psi)
+        recs = x.step(k)
+        field = x.copy2cpu().reshape(-1)
+    P = O.make_params(n, n, n, L=(L, L, L), a=q.a, b=q.b, sigma=q.sigma, peaks=FCC, envelope=1, ff_factor=DX ** 3,
+                      noise_amp=q.noise_amp, noise_seed=q.noise_seed)
+    ref, F, mean, rms = O.run(P, host_psi, k, k)
+    fin = [r for r in recs if r["iteration"] == k][0]
+    dev = field - field.mean()
+    return {"steps": k, "F_rel": abs(fin["F"] - F[k]) / abs(F[k]),
+            "field_rel_l2": float(np.linalg.norm(field - ref) / np.linalg.norm(ref)),
+            "deviation_rel_l2": float(np.linalg.norm(dev - (ref - ref.mean())) / np.linalg.norm(ref - ref.mean())),
+            "mean_abs_err": abs(fin["mean"] - mean[k]),
+            "against": "FP64 oracle on the host cores, same initial field and noise stream",
+            "bar": "F rel <= 1e-6, field rel-L2 <= 1e-5"}
+
+
+def reference_gpu_program(n, steps=101):
+    """LC2500/XPFC_CUDA's own program (baseline/ref_gpu.py, built for sm_103a
+    on this machine from its staged sources) at n^2, timed by its own TIMING
+    line over `steps` loop iterations with t_sample larger than the run (no
+    sampling inside the loop), as the reference times itself."""
+    try:
+        from baseline import ref_gpu
+    except ImportError as e:
+        return {"unavailable": "baseline/ref_gpu.py not importable: %s" % e}
+    prog = ref_gpu.programs()["xpfc_ref"]
+    if not os.path.exists(prog):
+        return {"unavailable": "the reference program is not built here (its sources are not staged)"}
+    import math as _m
+    dt = 0.25
+    t = (steps - 1) * dt
+    text = ("1 no_val\n0.05 0.25 psi_0 s\n1 3 0.1 1 a b eps Mo\n\n%d %d Lx Ly\n%d %d Mx My\n\n%g t\n%g dt\n"
+            "%d t_sample\n\n0 iconfig\n0.2 0.1 A_10 A_11\n0.3 A_tri\n\n1 iseed\n1 ishape\n4.0 4.0 6.0 h k roa\n"
+            % (n // 8, n // 8, n, n, t, dt, 10 ** 7))
+    r = ref_gpu.run(prog, text, 10 ** 7, keep_field=False, timeout=600)
+    ms = r["timing"].get("Full iteration time.")
+    iters = int(_m.ceil(t / dt + 1))
+    if r["returncode"] != 0 or not ms:
+        return {"unavailable": "the reference program failed (rc %d)" % r["returncode"]}
+    return {"value": n * n * iters / (ms / 1e3) / 1e9, "unit": UNIT, "loop_ms": ms, "loop_iterations": iters,
+            "what": "the reference's own main.cu loop (cuFFT Z2Z, FP64), its TIMING line, one GB300, "
+                    "cuFFT's multi-GPU descriptor calls served on one GPU (cufftXtSetGPUs refuses one GPU)"}
 
 
 def run_reference(args):
@@ -148,19 +204,20 @@ def run_reference(args):
                       ff_factor=DX ** 3, noise_amp=0.01, noise_seed=11)
     psi = O.ic_noise(n, n, n, 0.04, 0.05, 1)
     O.pin_mean(psi, 0.04)
-    # bounded sample: at most REF_MAX_STEPS timed and 1 warm-up step of the
-    # full-size workload (one 256^3 FP64 step takes ~0.25 s on 16 cores)
+    # bounded sample: at most REF_MAX_STEPS timed steps of the full-size
+    # workload (one 256^3 FP64 step takes ~0.25 s on 16 cores), after the same
+    # number of warm-up steps as the library's arm
     REF_MAX_STEPS = 40
     k = max(1, min(args.steps, REF_MAX_STEPS))
-    _, psi = O.bench(p, psi, 1)
+    _, psi = O.bench(p, psi, args.warmup)
     sec, _ = O.bench(p, psi, k)
     v = n ** 3 * k / sec / 1e9
-    cb = {"value": v, "unit": UNIT, "cores": O.threads(), "kind": "port",
-          "sample": "%d timed steps (+1 warm-up) of the %d^3 workload (of the %d requested), FP64 oracle "
+    cb = {"value": v, "unit": UNIT, "cores": O.threads(), "host_cpus": os.cpu_count(), "kind": "port",
+          "sample": "%d timed steps (+%d warm-up) of the %d^3 workload (of the %d requested), FP64 oracle "
                     "restating the reference loop (main.cu:306-435); the reference itself is CUDA-only"
-                    % (k, n, args.steps)}
+                    % (k, args.warmup, n, args.steps)}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": k, "warmup": 1, "ms_per_step": 1e3 * sec / k,
+            "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * sec / k,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, "mixed"),
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -235,6 +292,8 @@ def run_two_d(args, local, group, barrier):
             barrier()
             ms = group.max(e0.elapsed_time(e1))
         out[name] = {"value": group.sum(n * n * k) / (ms / 1e3) / 1e9, "ms_per_step": ms / k, "steps": k}
+    if not args.no_ref_gpu and group.rank == 0:
+        out["reference_program"] = reference_gpu_program(n)
     return out
 
 
@@ -303,6 +362,16 @@ def run_serve(args, rank, local, group, barrier):
                 f1 = x.copy2cpu()
             same &= bool(np.array_equal(f, f1) and r == r1)
     out = SV.summarise(recs, span, rate)
+    out["solves_per_s"] = len(recs) / span
+    if not args.no_serve_seq:
+        # the plain sequential baselines: the same requests one at a time, each
+        # alone, in FP64 and in mixed precision (estimated per grid size)
+        seq64 = SV.sequential_estimate(stream, X._lib.FP64)
+        seq32 = SV.sequential_estimate(stream, X._lib.MIXED)
+        out["sequential_fp64"] = seq64
+        out["sequential_mixed"] = seq32
+        out["solves_per_s_vs_sequential_fp64"] = out["solves_per_s"] / seq64["value"]
+        out["solves_per_s_vs_sequential_mixed"] = out["solves_per_s"] / seq32["value"]
     out.update({"unit": "s", "rate_per_s": rate, "max_running": args.serve_running, "chunk_steps": 16,
                 "hbm_budget_gb": budget / 2 ** 30, "peak_device_gb": stats["peak_bytes_in_use"] / 2 ** 30,
                 "contexts_created": stats["contexts_created"], "contexts_reused": stats["contexts_reused"],
@@ -436,8 +505,11 @@ def run_ours(args):
                 "step_frac_of_two_sweep_floor": (value * 1e9 / ws) * FLOOR_BYTES_PER_POINT / (peak * 1e9)}
 
     cpu = None
+    acc = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(n)
+        if args.precision == "mixed":
+            acc = accuracy(X, n, rank, local, host_psi, args.accuracy_steps)
 
     sweep = None
     if not args.no_sweep:
@@ -458,6 +530,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == X._lib.MIXED else "f64",
                 "data": "synthetic (seeded Philox initial field and noise)", "config": config(n, args.precision),
                 "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+                "accuracy": acc,
                 "fp64": fp64, "sweep": sweep, "serve": serve, "two_d": two_d}
         print(json.dumps(line), flush=True)
     x.close()
@@ -484,8 +557,11 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serve-running", type=int, default=16)
+    ap.add_argument("--no-serve-seq", action="store_true", help="skip the sequential baselines of the serve leg")
     ap.add_argument("--no-two-d", action="store_true")
     ap.add_argument("--two-d-size", type=int, default=4096)
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference program's 2-D timing")
+    ap.add_argument("--accuracy-steps", type=int, default=40)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -178,6 +178,25 @@ int xpfc_get_field(xpfc_ctx *ctx, double *host_psi);
 /* Current field of the fused state, as FP32 values on the device: the
    caller's device buffer of Mx*My*Mz floats (no host copy). */
 int xpfc_get_field_device_f32(xpfc_ctx *ctx, float *dev_out);
+/* copy_to_cpu.cu:3-18 without stopping the time loop (the reference copies
+   synchronously after the loop, main.cu:453): _async enqueues the transform of
+   the current field (the iteration after every step already enqueued) to real
+   space on the context stream and its device-to-host copy on a copy stream of
+   the context, and returns; steps enqueued after it run while the copy
+   proceeds.  _wait blocks until that copy is done and writes the field to
+   host_psi ([Mx][My][Mz] doubles) and its iteration to *iteration (may be
+   NULL).  One read-back at a time: a second _async drops an uncollected one. */
+int xpfc_get_field_async(xpfc_ctx *ctx);
+int xpfc_get_field_wait(xpfc_ctx *ctx, double *host_psi, long long *iteration);
+/* Checkpoint and resume of the fused state at full precision (the reference
+   restarts only from a 6-digit VTK field, read_input.cu:124-241, and lists
+   periodic checkpoints as to do, VERSIONLOG:8-10).  _save writes the spectral
+   state (both fused arrays, the iteration and the grid) to path; _load reads it
+   into a context of the same grid, precision and instance count, which then
+   continues bit for bit as the saved solve would have.  Both wait for the
+   context's stream. */
+int xpfc_save_state(xpfc_ctx *ctx, const char *path);
+int xpfc_load_state(xpfc_ctx *ctx, const char *path);
 
 /* ---- staged API: the reference's per-stage wrappers ---------------------
    FP64, reference semantics, buffers named by xpfc_buffer.                 */

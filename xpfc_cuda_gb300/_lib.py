@@ -95,6 +95,10 @@ SIGNATURES = [
     ("xpfc_iteration", C.c_longlong, [_ctx]),
     ("xpfc_get_field", C.c_int, [_ctx, _dp]),
     ("xpfc_get_field_device_f32", C.c_int, [_ctx, C.c_void_p]),
+    ("xpfc_get_field_async", C.c_int, [_ctx]),
+    ("xpfc_get_field_wait", C.c_int, [_ctx, _dp, C.POINTER(C.c_longlong)]),
+    ("xpfc_save_state", C.c_int, [_ctx, C.c_char_p]),
+    ("xpfc_load_state", C.c_int, [_ctx, C.c_char_p]),
     ("xpfc_upload", C.c_int, [_ctx, C.c_int, _dp]),
     ("xpfc_download", C.c_int, [_ctx, C.c_int, _dp]),
     ("xpfc_download_spectrum", C.c_int, [_ctx, C.c_int, _dp]),

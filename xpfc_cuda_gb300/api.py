@@ -198,6 +198,26 @@ class Xpfc:
     get_field = copy2cpu
 
     # ---- staged path: the reference's per-stage wrappers ---------------------
+    def copy2cpu_async(self):
+        """Starts reading the current field back (copy_to_cpu.cu:3-18) on the
+        context's copy stream; steps enqueued afterwards overlap the copy.
+        copy2cpu_wait() returns (field, iteration)."""
+        self._c(self._L.xpfc_get_field_async(self._h))
+
+    def copy2cpu_wait(self):
+        out = np.empty(self.ncells)
+        it = C.c_longlong()
+        self._c(self._L.xpfc_get_field_wait(self._h, _dp(out), C.byref(it)))
+        return out.reshape(self.shape), it.value
+
+    def save_state(self, path):
+        """Checkpoint of the fused state at full precision (xpfc_save_state)."""
+        self._c(self._L.xpfc_save_state(self._h, str(path).encode()))
+
+    def load_state(self, path):
+        """Resume from a checkpoint of the same grid and precision."""
+        self._c(self._L.xpfc_load_state(self._h, str(path).encode()))
+
     def upload(self, buf, host):
         a = np.ascontiguousarray(host, dtype=np.float64).reshape(-1)
         self._c(self._L.xpfc_upload(self._h, buf, _dp(a)))

@@ -1,5 +1,7 @@
 // xpfc_capi.cu -- the C ABI of libxpfc (include/xpfc.h): context, fused
 // step driver and the staged per-stage entry points.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -7,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -148,8 +151,36 @@ struct xpfc_ctx {
     size_t part_per_inst = 0;              // partial-sum doubles per instance
     // the xy passes of a 3-D step in plane chunks on auxiliary streams
     int xy_chunks = -1;                    // -1: not chosen yet
+    // pencil variant: 1 the staged (TMA) pass where it exists, 0 the register
+    // pass; chosen with xy_chunks by the autotuner (or the defaults)
+    int use_tma = 1;   // (the staged pass still needs XPFC_TMA=1, see tma_enabled)
+    bool tuned = false;
+    // captured step graph: GRAPH_STEPS plain iterations replayed by one graph
+    // launch, the first iteration read from a device word (d_step_base)
+    cudaGraphExec_t graph_exec = nullptr;
+    long long *d_step_base = nullptr;
+    const long long *cap_base = nullptr;   // set while a graph is being captured
+    int graph_state = 0;                   // 0: not built, 1: ready, -1: not used
+    bool graph_warm = false;               // a plain iteration ran pass by pass
+    int graph_chunks = -1;                 // the chunk count it was captured with
+    long long graph_kernels = 0;           // kernels in one replay
     cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t ev_fork = nullptr, ev_join[4] = {nullptr, nullptr, nullptr, nullptr};
+    // staged pencil pass of 3-D FP32 grids: tensor maps of S and W, the
+    // device word its blocks set when they give up waiting for a tile, and a
+    // pinned host copy of that word taken at the end of every step call
+    CUtensorMap tmS{}, tmW{};
+    // asynchronous read-back of the field (xpfc_get_field_async): a copy
+    // stream, the events that order it after the transform to real space and
+    // mark its end, a pinned host buffer and the iteration it holds
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_x_ready = nullptr, ev_copied = nullptr;
+    void *hfield = nullptr;
+    bool field_pending = false, copy_used = false;
+    long long field_iter = 0;
+    int tma_state = 0;                     // 0: not set up yet, 1: in use, -1: not used
+    int *dev_err = nullptr;
+    int *herr = nullptr;
 };
 
 enum { PASS_PENCIL = 0, PASS_COL_INV = 1, PASS_ROW = 2, PASS_COL_FWD = 3, PASS_RED = 4 };
@@ -187,10 +218,13 @@ static void drain_profile(xpfc_ctx *c) {
 
 static const char *kVersion = "xpfc-gb300 0.1 (sm_103a)";
 
+// (a failed call's error is also cleared from the thread's last-error state,
+// so that a later cudaGetLastError does not report it a second time)
 #define XPFC_CUDA(ctx, call)                                                                      \
     do {                                                                                          \
         cudaError_t e_ = (call);                                                                  \
         if (e_ != cudaSuccess) {                                                                  \
+            cudaGetLastError();                                                                   \
             (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                      \
             return XPFC_ECUDA;                                                                    \
         }                                                                                         \
@@ -637,6 +671,17 @@ extern "C" int xpfc_destroy(xpfc_ctx *ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->hslots) cudaFreeHost(ctx->hslots);
     if (ctx->hstage) cudaFreeHost(ctx->hstage);
+    cudaFree(ctx->dev_err);
+    if (ctx->herr) cudaFreeHost(ctx->herr);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    if (ctx->ev_x_ready) cudaEventDestroy(ctx->ev_x_ready);
+    if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
+    if (ctx->hfield) cudaFreeHost(ctx->hfield);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    cudaFree(ctx->d_step_base);
     for (int b = 0; b < XPFC_NBUF; b++) cudaFree(ctx->staged[b]);
     for (auto &e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -883,6 +928,67 @@ extern "C" int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi) {
 // ---------------------------------------------------------------------------
 // fused step
 // ---------------------------------------------------------------------------
+// The staged (TMA) pencil pass (xpfc_tma.cuh) for 3-D FP32 grids whose pencil
+// length has a staged instance, selected with XPFC_TMA=1 in the environment.
+// It is not the default: on GB300 at 256^3 it ran 138 us per launch against
+// the register pencil's 120 us, and the two kernels' results differ in the
+// last bits (the compiler contracts multiply-adds differently in each), so
+// they are not interchangeable within one solve.
+static bool tma_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("XPFC_TMA");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+
+// cuTensorMapEncodeTiled from the driver, through the runtime's entry-point
+// query (the library links no driver library itself)
+static PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }();
+    return fn;
+}
+
+// Tensor maps of S and W for boxes of tx complex columns x 1 row x the whole
+// pencil (length Lp), set up once per context; false: use the register pencil.
+static bool tma_ready(xpfc_ctx *ctx, int tx, int Lp) {
+    if (ctx->tma_state != 0) return ctx->tma_state > 0;
+    ctx->tma_state = -1;
+    if (!tma_enabled()) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)2 * ctx->L0, (cuuint64_t)ctx->n1, (cuuint64_t)ctx->n2 * ctx->nb};
+    const cuuint64_t strides[2] = {(cuuint64_t)2 * ctx->L0 * sizeof(float),
+                                   (cuuint64_t)2 * ctx->L0 * ctx->n1 * sizeof(float)};
+    const cuuint32_t box[3] = {(cuuint32_t)(2 * tx), 1u, (cuuint32_t)Lp};
+    const cuuint32_t es[3] = {1u, 1u, 1u};
+    for (int a = 0; a < 2; a++) {
+        const CUresult r = enc(a == 0 ? &ctx->tmS : &ctx->tmW, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                               a == 0 ? ctx->S : ctx->W, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return false;
+    }
+    if (cudaMalloc(&ctx->dev_err, sizeof(int)) != cudaSuccess) return false;
+    if (cudaMallocHost(&ctx->herr, sizeof(int)) != cudaSuccess) {
+        cudaFree(ctx->dev_err);
+        ctx->dev_err = nullptr;
+        return false;
+    }
+    *ctx->herr = 0;
+    if (cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream) != cudaSuccess) return false;
+    ctx->tma_state = 1;
+    return true;
+}
+
 template <typename T>
 static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int want_red, int *nb) {
     const bool dbl = sizeof(T) == 8;
@@ -891,6 +997,7 @@ static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int wan
     if (!twp) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
     KSpace ks = make_kspace(ctx, dbl);
     ks.step = step;
+    ks.step_base = ctx->cap_base;
     PenArgs pa{};
     pa.S = ctx->S;
     pa.W = ctx->W;
@@ -909,6 +1016,12 @@ static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int wan
     pa.nz = ctx->nb;
     const int npairs = ctx->three_d ? ctx->n1 / 2 + 1 : 1;
     ProfScope ps(ctx, PASS_PENCIL);
+    const int ttx = (ctx->three_d && sizeof(T) == 4) ? pen_tma_tx(Lp, 4) : 0;
+    if (ctx->use_tma && ttx > 0 && ctx->L0 % ttx == 0 && tma_ready(ctx, ttx, Lp)) {
+        XPFC_LAUNCH(ctx, launch_pencil_tma<T>(Lp, pa, ks, npairs, twp, &ctx->tmS, &ctx->tmW, ctx->dev_err,
+                                              ctx->stream, nb));
+        return XPFC_OK;
+    }
     XPFC_LAUNCH(ctx, launch_pencil<T>(Lp, ctx->three_d ? 2 : 1, pa, ks, npairs, twp, ctx->stream, nb));
     return XPFC_OK;
 }
@@ -918,22 +1031,31 @@ static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int wan
 // row pass to the y-forward pass, and the chunks run on four auxiliary
 // streams, so the passes of neighbouring chunks overlap on the SMs.
 // XPFC_XY_CHUNKS overrides the choice.
+// Auxiliary streams and events of the chunked xy passes (created once).
+static bool ensure_aux(xpfc_ctx *ctx) {
+    if (ctx->ev_fork) return true;
+    for (int k = 0; k < 4; k++)
+        if (cudaStreamCreateWithFlags(&ctx->aux[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_join[k], cudaEventDisableTiming) != cudaSuccess)
+            return false;
+    return cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+}
+
+// The default chunk count (before or without tuning): four chunks for 3-D
+// states of at least 32 MB whose slow axis divides by four.
+static int xy_default_chunks(const xpfc_ctx *ctx) {
+    const size_t slab = ctx->esz * (size_t)ctx->ncells * ctx->nb;
+    return (ctx->three_d && ctx->n2 % 4 == 0 && ctx->n2 >= 64 && slab >= ((size_t)32 << 20)) ? 4 : 1;
+}
+
 static int xy_chunk_count(xpfc_ctx *ctx) {
     if (ctx->xy_chunks >= 0) return ctx->xy_chunks;
-    int c = 1;
-    const size_t slab = ctx->esz * (size_t)ctx->ncells * ctx->nb;
-    if (ctx->three_d && ctx->n2 % 4 == 0 && ctx->n2 >= 64 && slab >= ((size_t)32 << 20)) c = 4;
+    int c = xy_default_chunks(ctx);
     if (const char *e = getenv("XPFC_XY_CHUNKS")) {
         const int v = atoi(e);
         if (v >= 1 && ctx->n2 % v == 0) c = v;
     }
-    if (c > 1) {
-        for (int k = 0; k < 4 && c > 1; k++)
-            if (cudaStreamCreateWithFlags(&ctx->aux[k], cudaStreamNonBlocking) != cudaSuccess ||
-                cudaEventCreateWithFlags(&ctx->ev_join[k], cudaEventDisableTiming) != cudaSuccess)
-                c = 1;
-        if (c > 1 && cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess) c = 1;
-    }
+    if (c > 1 && !ensure_aux(ctx)) c = 1;
     ctx->xy_chunks = c;
     return c;
 }
@@ -1076,12 +1198,251 @@ static int enqueue_begin(xpfc_ctx *ctx, long long nsteps, bool final_F) {
     return XPFC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// autotuner of the step's schedule
+// ---------------------------------------------------------------------------
+// The schedule of a 3-D step: the number of plane chunks of the xy passes
+// (1, 2, 4 or 8; chunks run on four auxiliary streams and keep their slab in
+// L2 between passes).  Every candidate runs the same kernels on the same
+// data, so all give the same bits, and the tuner times them on the solve's
+// own first plain iterations: each candidate runs one untimed and TUNE_STEPS
+// timed iterations between CUDA events, the fastest is kept for the context
+// and remembered for its shape (grid, instances, precision, device) in a
+// process-wide table, so later contexts of that shape start with it.
+// XPFC_AUTOTUNE=0 keeps the defaults; XPFC_XY_CHUNKS fixes the chunk count.
+struct Sched {
+    int chunks, tma;
+};
+static std::mutex g_sched_mu;
+static std::map<std::string, Sched> g_sched;
+constexpr int TUNE_STEPS = 6;
+
+static std::string sched_key(const xpfc_ctx *ctx) {
+    return std::to_string(ctx->n0) + "x" + std::to_string(ctx->n1) + "x" + std::to_string(ctx->n2) + "/" +
+           std::to_string(ctx->nb) + "/" + std::to_string(ctx->esz) + "/" + std::to_string(ctx->p.device);
+}
+
+static bool autotune_on() {
+    static const bool on = [] {
+        const char *e = getenv("XPFC_AUTOTUNE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+static std::vector<Sched> sched_candidates(xpfc_ctx *ctx) {
+    std::vector<Sched> out;
+    std::vector<int> chunks = {1};
+    if (!getenv("XPFC_XY_CHUNKS") && ensure_aux(ctx))
+        for (int c : {2, 4, 8})
+            if (ctx->n2 % c == 0 && ctx->n2 / c >= 8) chunks.push_back(c);
+    for (int c : chunks) out.push_back({c, ctx->use_tma});
+    return out;
+}
+
+static void sched_apply(xpfc_ctx *ctx, Sched s) {
+    // chunked xy passes need the auxiliary streams of this context
+    ctx->xy_chunks = (s.chunks > 1 && !ensure_aux(ctx)) ? 1 : s.chunks;
+    ctx->use_tma = s.tma;
+}
+
+// A plain iteration (no diagnostics produced by it or by the next one).
+static bool plain_iter(const xpfc_ctx *ctx, long long i) {
+    return !(diag_wantF(ctx, i) || diag_wantR(ctx, i) || diag_wantF(ctx, i + 1));
+}
+
+template <typename T>
+static int plain_step(xpfc_ctx *ctx, long long i) {
+    int nb = 0;
+    int rc = launch_pencil_pass<T>(ctx, i, 1, 0, &nb);
+    if (rc == XPFC_OK) rc = launch_xy_pass<T>(ctx, 0, &nb);
+    return rc;
+}
+
+// Schedule of the context before its first step: the remembered one for its
+// shape, or the defaults.  Returns true when the context still has to tune.
+static bool sched_init(xpfc_ctx *ctx) {
+    if (ctx->tuned) return false;
+    if (!ctx->three_d || !autotune_on() || ctx->profiling) {
+        ctx->tuned = true;
+        return false;
+    }
+    std::lock_guard<std::mutex> g(g_sched_mu);
+    auto it = g_sched.find(sched_key(ctx));
+    if (it != g_sched.end()) {
+        sched_apply(ctx, it->second);
+        ctx->tuned = true;
+        return false;
+    }
+    return true;
+}
+
+// Runs the candidates on iterations [i, i + n) (all plain; n = candidates x
+// (TUNE_STEPS + 1)) and keeps the fastest.  Returns the next iteration.
+template <typename T>
+static int autotune(xpfc_ctx *ctx, long long &i) {
+    const std::vector<Sched> cand = sched_candidates(ctx);
+    std::vector<cudaEvent_t> ev(2 * cand.size(), nullptr);
+    for (auto &e : ev) XPFC_CUDA(ctx, cudaEventCreate(&e));
+    int rc = XPFC_OK;
+    for (size_t c = 0; c < cand.size() && rc == XPFC_OK; c++) {
+        sched_apply(ctx, cand[c]);
+        rc = plain_step<T>(ctx, i++);   // untimed: first launches, tables, tensor maps
+        if (rc != XPFC_OK) break;
+        XPFC_CUDA(ctx, cudaEventRecord(ev[2 * c], ctx->stream));
+        for (int k = 0; k < TUNE_STEPS && rc == XPFC_OK; k++) rc = plain_step<T>(ctx, i++);
+        XPFC_CUDA(ctx, cudaEventRecord(ev[2 * c + 1], ctx->stream));
+    }
+    if (rc == XPFC_OK) {
+        XPFC_CUDA(ctx, cudaEventSynchronize(ev.back()));
+        size_t best = 0;
+        float best_ms = 0.f;
+        for (size_t c = 0; c < cand.size(); c++) {
+            float ms = 0.f;
+            XPFC_CUDA(ctx, cudaEventElapsedTime(&ms, ev[2 * c], ev[2 * c + 1]));
+            if (c == 0 || ms < best_ms) {
+                best = c;
+                best_ms = ms;
+            }
+        }
+        sched_apply(ctx, cand[best]);
+        ctx->tuned = true;
+        std::lock_guard<std::mutex> g(g_sched_mu);
+        g_sched[sched_key(ctx)] = cand[best];
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// step graphs
+// ---------------------------------------------------------------------------
+// Runs of GRAPH_STEPS plain iterations (after the schedule is tuned) are
+// replayed from one captured CUDA graph: the passes of those iterations with
+// their programmatic dependences and the fork/join of the chunked xy passes.
+// The noise of an iteration depends on its index, which the pencil passes read
+// as (device word) + (their position in the graph); a one-thread kernel sets
+// the word before each replay.  The graph is built once per context and
+// schedule, and dropped when the context takes new params.  XPFC_GRAPH=0
+// launches every pass on its own.
+constexpr int GRAPH_STEPS = 16;
+
+static bool graphs_on() {
+    static const bool on = [] {
+        const char *e = getenv("XPFC_GRAPH");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+__global__ void set_step_base_kernel(long long *p, long long v) { *p = v; }
+
+static void drop_graph(xpfc_ctx *ctx) {
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+    ctx->graph_state = 0;
+}
+
+// Captures GRAPH_STEPS plain iterations; on any failure the context keeps
+// launching pass by pass (graph_state -1).
+template <typename T>
+static int graph_build(xpfc_ctx *ctx) {
+    drop_graph(ctx);
+    ctx->graph_state = -1;
+    if (!ctx->d_step_base && cudaMalloc(&ctx->d_step_base, sizeof(long long)) != cudaSuccess) {
+        ctx->d_step_base = nullptr;
+        cudaGetLastError();
+        return XPFC_OK;
+    }
+    const long long l0 = ctx->launches;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        cudaGetLastError();
+        return XPFC_OK;
+    }
+    ctx->cap_base = ctx->d_step_base;
+    int rc = XPFC_OK;
+    for (int j = 0; j < GRAPH_STEPS && rc == XPFC_OK; j++) rc = plain_step<T>(ctx, j);
+    ctx->cap_base = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    const long long kernels = ctx->launches - l0;
+    ctx->launches = l0;   // a capture launches nothing
+    if (rc != XPFC_OK || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        ctx->err.clear();
+        return XPFC_OK;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        ctx->graph_exec = nullptr;
+        cudaGetLastError();
+        return XPFC_OK;
+    }
+    ctx->graph_state = 1;
+    ctx->graph_chunks = ctx->xy_chunks;
+    ctx->graph_kernels = kernels;
+    return XPFC_OK;
+}
+
+// Replays the graph for iterations [i, i + GRAPH_STEPS) when it can.
+template <typename T>
+static int graph_try(xpfc_ctx *ctx, long long i, long long i1, bool &done) {
+    done = false;
+    if (!graphs_on() || !ctx->tuned || ctx->profiling || i + GRAPH_STEPS > i1) return XPFC_OK;
+    for (long long j = i; j < i + GRAPH_STEPS; j++)
+        if (!plain_iter(ctx, j)) return XPFC_OK;
+    if (ctx->graph_state == 1 && ctx->graph_chunks != ctx->xy_chunks) drop_graph(ctx);
+    if (ctx->graph_state == 0) {
+        // the first plain iteration of a context runs pass by pass: it makes
+        // the tables, streams and kernel set-up a capture must not create
+        if (!ctx->graph_warm) {
+            ctx->graph_warm = true;
+            return XPFC_OK;
+        }
+        int rc = graph_build<T>(ctx);
+        if (rc != XPFC_OK) return rc;
+    }
+    if (ctx->graph_state != 1) return XPFC_OK;
+    set_step_base_kernel<<<1, 1, 0, ctx->stream>>>(ctx->d_step_base, i);
+    XPFC_CUDA(ctx, cudaGetLastError());
+    XPFC_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->launches += 1 + ctx->graph_kernels;
+    done = true;
+    return XPFC_OK;
+}
+
 template <typename T>
 static int enqueue_steps(xpfc_ctx *ctx, long long i0, long long i1) {
     std::map<long long, int> &slot = ctx->diag_slot;
     const int nbi = ctx->nb;
     const long long sstride = 8LL * (long long)ctx->diag_its.size();
+    bool tune = sched_init(ctx);
     for (long long i = i0; i < i1; i++) {
+        if (tune) {
+            // tune on the first run of enough plain iterations
+            const long long need = (long long)sched_candidates(ctx).size() * (TUNE_STEPS + 1);
+            bool ok = need > 1 && i + need <= i1;
+            for (long long j = i; ok && j < i + need; j++) ok = plain_iter(ctx, j);
+            if (ok) {
+                long long j = i;
+                const int rc = autotune<T>(ctx, j);
+                if (rc != XPFC_OK) return rc;
+                tune = false;
+                i = j - 1;
+                continue;
+            }
+        }
+        {
+            bool replayed = false;
+            const int rc = graph_try<T>(ctx, i, i1, replayed);
+            if (rc != XPFC_OK) return rc;
+            if (replayed) {
+                i += GRAPH_STEPS - 1;
+                continue;
+            }
+        }
         const bool red = diag_wantF(ctx, i) || diag_wantR(ctx, i);
         int nb = 0;
         int rc = launch_pencil_pass<T>(ctx, i, 1, red ? 1 : 0, &nb);
@@ -1121,6 +1482,8 @@ static int enqueue_end(xpfc_ctx *ctx) {
     if (ns > 0)
         XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->hslots, ctx->slots, sizeof(double) * 8 * ns * nbi,
                                        cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->dev_err)
+        XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->herr, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->iteration = fin;
     ctx->diag_pending = true;
     return XPFC_OK;
@@ -1139,6 +1502,8 @@ static int fused_enqueue(xpfc_ctx *ctx, long long nsteps, bool final_F) {
 static int collect_inst(xpfc_ctx *ctx, int k, xpfc_diag *out, int cap, int *count) {
     if (count) *count = 0;
     if (!ctx->diag_pending) return XPFC_OK;
+    if (ctx->herr && *ctx->herr)
+        return fail(ctx, XPFC_ETIMEDOUT, "a pencil block gave up waiting for its staged tile (bounded wait)");
     const xpfc_params &p = ctx->inst[k];
     const double N = (double)ctx->ncells;
     const size_t ns = ctx->diag_its.size();
@@ -1221,6 +1586,8 @@ template <typename T>
 static int field_to_X(xpfc_ctx *ctx, int k = 0) {
     const bool dbl = sizeof(T) == 8;
     void *Sk = (char *)ctx->S + ctx->esz * (size_t)ctx->ncells * k;
+    // an asynchronous read-back may still be copying X to the host
+    if (ctx->copy_used) XPFC_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0));
     if (!ctx->X) {
         XPFC_CUDA(ctx, cudaMalloc(&ctx->X, ctx->esz * (size_t)ctx->ncells));
         poison(ctx->X, ctx->esz * (size_t)ctx->ncells, ctx->stream);
@@ -1281,6 +1648,119 @@ extern "C" int xpfc_get_field_device_f32(xpfc_ctx *ctx, float *dev_out) {
     else
         XPFC_LAUNCH(ctx, launch_convert_d2f((const double *)ctx->X, dev_out, n, ctx->stream));
     XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_get_field_async(xpfc_ctx *ctx) {
+    if (!ctx) return fail(nullptr, XPFC_EINVAL, "null context");
+    if (!ctx->initialized) return fail(ctx, XPFC_ESTATE, "no field before xpfc_initialize");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    if (!ctx->copy_stream) {
+        XPFC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        XPFC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_x_ready, cudaEventDisableTiming));
+        XPFC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming));
+        XPFC_CUDA(ctx, cudaMallocHost(&ctx->hfield, ctx->esz * (size_t)ctx->ncells));
+    }
+    // a read-back that was never collected is dropped; its copy finishes first
+    int rc = ctx->esz == 4 ? field_to_X<float>(ctx) : field_to_X<double>(ctx);
+    if (rc != XPFC_OK) return rc;
+    XPFC_CUDA(ctx, cudaEventRecord(ctx->ev_x_ready, ctx->stream));
+    XPFC_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_x_ready, 0));
+    XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->hfield, ctx->X, ctx->esz * (size_t)ctx->ncells, cudaMemcpyDeviceToHost,
+                                   ctx->copy_stream));
+    XPFC_CUDA(ctx, cudaEventRecord(ctx->ev_copied, ctx->copy_stream));
+    ctx->copy_used = true;
+    ctx->field_pending = true;
+    ctx->field_iter = ctx->iteration;
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_get_field_wait(xpfc_ctx *ctx, double *host_psi, long long *iteration) {
+    if (!ctx || !host_psi) return fail(ctx, XPFC_EINVAL, "null argument");
+    if (!ctx->field_pending) return fail(ctx, XPFC_ESTATE, "no read-back requested (xpfc_get_field_async)");
+    XPFC_CUDA(ctx, cudaEventSynchronize(ctx->ev_copied));
+    const size_t n = (size_t)ctx->ncells;
+    if (ctx->esz == 4) widen((const float *)ctx->hfield, host_psi, n);
+    else memcpy(host_psi, ctx->hfield, sizeof(double) * n);
+    if (iteration) *iteration = ctx->field_iter;
+    ctx->field_pending = false;
+    return XPFC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// state snapshots: the fused state (S and W) at full precision
+// ---------------------------------------------------------------------------
+namespace {
+struct SnapHeader {
+    char magic[8];            // "XPFCSNP1"
+    int32_t esz, nb, Mx, My, Mz, pad;
+    int64_t iteration;
+    int64_t bytes;            // bytes of S (and of W)
+    double psi0;
+};
+}  // namespace
+
+extern "C" int xpfc_save_state(xpfc_ctx *ctx, const char *path) {
+    if (!ctx || !path) return fail(ctx, XPFC_EINVAL, "null argument");
+    if (!ctx->initialized) return fail(ctx, XPFC_ESTATE, "no state before xpfc_initialize");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    const size_t bytes = ctx->esz * (size_t)ctx->ncells * ctx->nb;
+    int rc = host_stage(ctx, 2 * bytes);
+    if (rc != XPFC_OK) return rc;
+    char *h = static_cast<char *>(ctx->hstage);
+    XPFC_CUDA(ctx, cudaMemcpyAsync(h, ctx->S, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    XPFC_CUDA(ctx, cudaMemcpyAsync(h + bytes, ctx->W, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SnapHeader hd{};
+    memcpy(hd.magic, "XPFCSNP1", 8);
+    hd.esz = (int32_t)ctx->esz;
+    hd.nb = ctx->nb;
+    hd.Mx = ctx->p.Mx;
+    hd.My = ctx->p.My;
+    hd.Mz = ctx->p.Mz;
+    hd.iteration = ctx->iteration;
+    hd.bytes = (int64_t)bytes;
+    hd.psi0 = ctx->p.psi0;
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(ctx, XPFC_EIO, std::string("cannot open ") + path);
+    const bool ok = fwrite(&hd, sizeof(hd), 1, f) == 1 && fwrite(h, 1, 2 * bytes, f) == 2 * bytes;
+    if (fclose(f) != 0 || !ok) return fail(ctx, XPFC_EIO, std::string("write failed: ") + path);
+    return XPFC_OK;
+}
+
+extern "C" int xpfc_load_state(xpfc_ctx *ctx, const char *path) {
+    if (!ctx || !path) return fail(ctx, XPFC_EINVAL, "null argument");
+    XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(ctx, XPFC_EIO, std::string("cannot open ") + path);
+    SnapHeader hd{};
+    const size_t bytes = ctx->esz * (size_t)ctx->ncells * ctx->nb;
+    if (fread(&hd, sizeof(hd), 1, f) != 1 || memcmp(hd.magic, "XPFCSNP1", 8) != 0) {
+        fclose(f);
+        return fail(ctx, XPFC_EIO, std::string("not a state snapshot: ") + path);
+    }
+    if (hd.esz != (int32_t)ctx->esz || hd.nb != ctx->nb || hd.Mx != ctx->p.Mx || hd.My != ctx->p.My ||
+        hd.Mz != ctx->p.Mz || hd.bytes != (int64_t)bytes) {
+        fclose(f);
+        return fail(ctx, XPFC_EINVAL, "the snapshot's grid, precision or instance count differs from the context's");
+    }
+    int rc = host_stage(ctx, 2 * bytes);
+    if (rc != XPFC_OK) {
+        fclose(f);
+        return rc;
+    }
+    char *h = static_cast<char *>(ctx->hstage);
+    // the staging buffer may still feed an upload enqueued earlier
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const bool ok = fread(h, 1, 2 * bytes, f) == 2 * bytes;
+    fclose(f);
+    if (!ok) return fail(ctx, XPFC_EIO, std::string("truncated snapshot: ") + path);
+    XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->S, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->W, h + bytes, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->iteration = hd.iteration;
+    ctx->initialized = true;
+    ctx->diag_pending = false;
     return XPFC_OK;
 }
 

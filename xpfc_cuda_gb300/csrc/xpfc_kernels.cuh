@@ -332,6 +332,9 @@ struct KSpace {
     unsigned long long noise_seed;
     const unsigned long long *seeds; // per batched instance (null: noise_seed)
     long long step;
+    // a step call replayed from a captured graph reads its first iteration
+    // from this device word and adds step (null: step alone)
+    const long long *step_base;
     // the same constants in FP32 for the mixed path (no FP64 work per mode)
     float f_dk0sq, f_dk1sq, f_dk2sq, f_dt, f_Mo, f_eps, f_noise_scale;
     float f_pk_k[8], f_pk_inv2a2[8], f_pk_dw[8];
@@ -345,16 +348,25 @@ template <typename T> struct Coef { T A, B, c2, k2; };
 struct Inst {
     const void *table;
     unsigned long long seed;
+    unsigned long long nstream;   // Philox stream word of this iteration's noise: 1 + iteration
+    double pin;   // the pinned k = 0 value (pencil passes; set by the kernel)
 };
+// instance z of a batched launch
 template <typename T>
-__device__ __forceinline__ Inst inst_of(const KSpace &k) {
+__device__ __forceinline__ Inst inst_at(const KSpace &k, int z) {
     Inst r;
     r.table = k.table;
     r.seed = k.noise_seed;
+    r.pin = 0.0;
+    r.nstream = 1ull + (unsigned long long)(k.step + (k.step_base ? *k.step_base : 0ll));
     if (k.tstride && k.table)
-        r.table = reinterpret_cast<const char *>(k.table) + (size_t)blockIdx.z * k.tstride * 4 * sizeof(T);
-    if (k.seeds) r.seed = k.seeds[blockIdx.z];
+        r.table = reinterpret_cast<const char *>(k.table) + (size_t)z * k.tstride * 4 * sizeof(T);
+    if (k.seeds) r.seed = k.seeds[z];
     return r;
+}
+template <typename T>
+__device__ __forceinline__ Inst inst_of(const KSpace &k) {
+    return inst_at<T>(k, blockIdx.z);
 }
 
 __device__ __forceinline__ int signed_idx(int i, int n) { return 2 * i <= n ? i : i - n; }
@@ -446,8 +458,8 @@ __device__ __forceinline__ void box_muller_half(uint32_t a, uint32_t b, float &g
 // Philox draw for a canonical mode (c0, c1, c2): the slowest axis (z in 3-D,
 // y in 2-D) is folded in half; the lower half takes outputs 0,1, the upper 2,3.
 template <bool ROLLED = true>
-__device__ __forceinline__ uint4 noise_draw(const KSpace &ks, unsigned long long seed, int c0, int c1, int c2,
-                                            bool &upper) {
+__device__ __forceinline__ uint4 noise_draw(const KSpace &ks, unsigned long long seed, unsigned long long stream,
+                                            int c0, int c1, int c2, bool &upper) {
     // the counter is below n0 n1 n2 / 2, which fits in 32 bits for every
     // supported grid (at most 2^27 cells), so its upper word is 0
     uint32_t ctr;
@@ -460,7 +472,6 @@ __device__ __forceinline__ uint4 noise_draw(const KSpace &ks, unsigned long long
         const int f1 = upper ? c1 - ks.n1 / 2 : c1;
         ctr = (uint32_t)f1 * (uint32_t)ks.n0 + (uint32_t)c0;
     }
-    const unsigned long long stream = 1ull + (unsigned long long)ks.step;
     return philox4x32_10<ROLLED>(make_uint4(ctr, 0u, (uint32_t)stream, (uint32_t)(stream >> 32)),
                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
 }
@@ -473,14 +484,16 @@ template <typename T> __device__ __forceinline__ T noise_amp_of(const KSpace &ks
 // conserved noise xi_k = amp sqrt(cells) |k| g_k at full-grid mode (i0,i1,i2),
 // i0 in [0, n0/2]; Hermitian pairing as the oracle defines it
 template <typename T>
-__device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, unsigned long long seed, int i0, int i1, int i2, T k2) {
+__device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, unsigned long long seed, unsigned long long stream, int i0,
+                                            int i1, int i2, T k2) {
     const int j1 = (ks.n1 - i1) % ks.n1, j2 = (ks.n2 - i2) % ks.n2;
     const bool edge = (i0 == 0) || (2 * i0 == ks.n0);
     const bool selfc = edge && j1 == i1 && j2 == i2;
     bool canon = true;
     if (edge) canon = (long long)i2 * ks.n1 + i1 <= (long long)j2 * ks.n1 + j1;
     bool upper;
-    const uint4 o = canon ? noise_draw(ks, seed, i0, i1, i2, upper) : noise_draw(ks, seed, i0, j1, j2, upper);
+    const uint4 o =
+        canon ? noise_draw(ks, seed, stream, i0, i1, i2, upper) : noise_draw(ks, seed, stream, i0, j1, j2, upper);
     T g0, g1;
     box_muller<T>(upper ? o.z : o.x, upper ? o.w : o.y, g0, g1);
     const T amp = noise_amp_of<T>(ks, k2);
@@ -494,10 +507,10 @@ __device__ __forceinline__ cplx<T> noise_at(const KSpace &ks, unsigned long long
 // output, each complex Gaussian scaled by 1/sqrt 2 (the mode amplitude
 // noise_amp_of(k^2) multiplies it where the coefficients are at hand).
 template <typename T>
-__device__ __forceinline__ void noise_pair_unit(const KSpace &ks, unsigned long long seed, int i0, int i1, int i2,
-                                                cplx<T> &ga, cplx<T> &gb) {
+__device__ __forceinline__ void noise_pair_unit(const KSpace &ks, unsigned long long seed, unsigned long long stream,
+                                                int i0, int i1, int i2, cplx<T> &ga, cplx<T> &gb) {
     bool upper;
-    const uint4 o = noise_draw<false>(ks, seed, i0, i1, i2, upper);
+    const uint4 o = noise_draw<false>(ks, seed, stream, i0, i1, i2, upper);
     if constexpr (sizeof(T) == 4) {
         float g0, g1, g2, g3;
         box_muller_half(o.x, o.y, g0, g1);
@@ -609,7 +622,7 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
         if (slot != 0) {
             Coef<T> cf = kcoef<T>(ks, in.table, slot, i1, i2);
             cplx<T> num = xs;
-            if (ks.noise_on) num = cadd(num, noise_at<T>(ks, in.seed, slot, i1, i2, cf.k2));
+            if (ks.noise_on) num = cadd(num, noise_at<T>(ks, in.seed, in.nstream, slot, i1, i2, cf.k2));
             cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
             if (args.want_red) {
                 const double xr = xs.x, xi = xs.y;
@@ -635,8 +648,8 @@ pencil_kernel(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twL) {
             const Coef<T> c0 = kcoef<T>(ks, in.table, 0, i1, i2), cN = kcoef<T>(ks, in.table, nh, i1, i2);
             cplx<T> num0 = s0, numN = sN;
             if (ks.noise_on) {
-                num0 = cadd(num0, noise_at<T>(ks, in.seed, 0, i1, i2, c0.k2));
-                numN = cadd(numN, noise_at<T>(ks, in.seed, nh, i1, i2, cN.k2));
+                num0 = cadd(num0, noise_at<T>(ks, in.seed, in.nstream, 0, i1, i2, c0.k2));
+                numN = cadd(numN, noise_at<T>(ks, in.seed, in.nstream, nh, i1, i2, cN.k2));
             }
             cplx<T> x0n = mk<T>(c0.A * num0.x + c0.B * w0.x, c0.A * num0.y + c0.B * w0.y);
             cplx<T> xNn = mk<T>(cN.A * numN.x + cN.B * wN.x, cN.A * numN.y + cN.B * wN.y);

@@ -3,10 +3,12 @@
 // dispatches the runtime line length to its compile-time instance and
 // returns cudaErrorInvalidValue for a length that has none.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "xpfc_kernels.cuh"
 #include "xpfc_regkernels.cuh"
+#include "xpfc_tma.cuh"
 #include "xpfc_ic.cuh"
 
 namespace xpfc {
@@ -24,6 +26,17 @@ cudaError_t launch_col(int dir, int L, const ColArgs &a, int nouter, const void 
 template <typename T>
 cudaError_t launch_pencil(int L, int ng, const PenArgs &a, const KSpace &ks, int npairs, const void *twL,
                           cudaStream_t s, int *nblocks);
+// The staged pencil pass of 3-D grids (xpfc_tma.cuh): a persistent kernel fed
+// by TMA box loads of S and W through mapS / mapW (FP32 arrays
+// [n2 * instances][n1][n0], boxes of [L][2 tx][1]).  pen_tma_tx gives the
+// tile width in complex columns for a pencil length (0: no staged instance
+// for that length and element size); the pass needs L0 % tx == 0.  err: a
+// device word that a block which gave up waiting sets to XPFC_DEV_ETIMEDOUT.
+int pen_tma_tx(int L, int esz);
+template <typename T>
+cudaError_t launch_pencil_tma(int L, const PenArgs &a, const KSpace &ks, int npairs, const void *twL,
+                              const CUtensorMap *mapS, const CUtensorMap *mapW, int *err, cudaStream_t s,
+                              int *nblocks);
 template <typename T>
 cudaError_t launch_kspace(int op, const KSpace &ks, double a, double b, void *out, const void *x1, const void *x2,
                           const void *x3, const void *x4, cudaStream_t s);

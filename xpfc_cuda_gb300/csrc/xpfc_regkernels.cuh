@@ -42,6 +42,25 @@ template <int NQ> struct DSum<float, NQ> {
     __device__ __forceinline__ double get(int q) const { return (double)s[q] - (double)c[q]; }
 };
 
+// Pitch (complex elements) between the transpose scratch of lines that sit
+// side by side in a warp.  Shared memory serves a 64-bit access per half-warp
+// (FP32 complex) and a 128-bit access per quarter-warp (FP64) in one
+// wavefront when those G lanes (G = 16 or 8) touch the 32 banks once.  In the
+// column and pencil passes the G lanes are TX columns times G/TX consecutive
+// threads of a line, whose slots are consecutive, so line l must start G/TX
+// slots (mod G) after line l - 1; in the row pass the G lanes are G/Q rows
+// times Q consecutive threads, so rows start Q slots (mod G) apart.  (A pitch
+// of 2 mod 16 served the 8-column pencils but made every 16-column column
+// pass take two wavefronts per access.)
+template <typename T, int N, int TX> constexpr int line_pitch() {
+    constexpr int G = sizeof(T) == 4 ? 16 : 8;
+    return RPad<N>::template pitch<G, TX >= G ? 1 : (G / TX) % G>();
+}
+template <typename T, int N> constexpr int row_pitch() {
+    constexpr int G = sizeof(T) == 4 ? 16 : 8;
+    return RPad<N>::template pitch<G, RP<N>::Q % G>();
+}
+
 // ---------------------------------------------------------------------------
 // column pass (C2C along a strided axis), TX columns per block
 // ---------------------------------------------------------------------------
@@ -52,7 +71,7 @@ template <typename T, int N> struct RColShape {
     static constexpr int TXd = sizeof(T) == 4 ? 16 : 8, MAXT = sizeof(T) == 4 ? 1024 : 512;
     static constexpr int TX = TXd * Q > MAXT ? MAXT / Q : TXd;
     static constexpr int THREADS = TX * Q;
-    static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
+    static constexpr int LP = line_pitch<T, N, TX>();
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + (size_t)TX * LP);
 };
 
@@ -97,7 +116,7 @@ template <typename T, int N> struct RRowShape {
     static constexpr int Q = RP<N>::Q, P = RP<N>::P;
     static constexpr int ROWS = 256 / Q;
     static constexpr int THREADS = ROWS * Q;
-    static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 8>() : RPad<N>::template pitch<2, 1>();
+    static constexpr int LP = row_pitch<T, N>();
     static constexpr size_t SMEM = sizeof(cplx<T>) * (2 * N + (size_t)ROWS * LP) + sizeof(double) * 32 * NQ_ROW;
 };
 
@@ -249,7 +268,7 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int TX = RP<N>::three ? (Q >= 256 ? 2 : (sizeof(T) == 4 || NG == 1) ? 4 : 2)
                                            : (sizeof(T) == 4 ? 8 : 4) * ((Q == 4 && N >= 96) ? 2 : 1);
     static constexpr int THREADS = TX * Q * NG;
-    static constexpr int LP = sizeof(T) == 4 ? RPad<N>::template pitch<16, 2>() : RPad<N>::template pitch<2, 1>();
+    static constexpr int LP = line_pitch<T, N, TX>();
     static constexpr int LINES = TX * NG;
     static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
     // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
@@ -304,10 +323,10 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const Inst &in,
                                                int i2, cplx<T> xs, cplx<T> xw, DSum<T, NQ_PEN> &acc, T weight) {
     const Coef<T> cf = kcoef<T>(ks, in.table, i0, i1, i2);
     cplx<T> noise = mk<T>((T)0, (T)0);
-    if (ks.noise_on) noise = noise_at<T>(ks, in.seed, i0, i1, i2, cf.k2);
+    if (ks.noise_on) noise = noise_at<T>(ks, in.seed, in.nstream, i0, i1, i2, cf.k2);
     const cplx<T> num = cadd(xs, noise);
     cplx<T> xn = mk<T>(cf.A * num.x + cf.B * xw.x, cf.A * num.y + cf.B * xw.y);
-    if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)pin_of(args), (T)0);
+    if (args.pin && i0 == 0 && i1 == 0 && i2 == 0) xn = mk<T>((T)in.pin, (T)0);
     if (args.want_red) diag_mode<T>(ks, cf, xs, xw, noise, xn, acc, weight);
     return xn;
 }
@@ -315,7 +334,8 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const Inst &in,
 template <typename T, int N, int NG, bool RED>
 __global__ void __launch_bounds__(RPenShape<T, N, NG>::THREADS, RPenShape<T, N, NG>::MINB)
 pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
-    const Inst in = inst_of<T>(ks);
+    Inst in = inst_of<T>(ks);
+    in.pin = pin_of(args);
     using S = RPenShape<T, N, NG>;
     constexpr int TX = S::TX, Q = S::Q, P = S::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -439,7 +459,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
                 const int kza = t + Q * j;
                 const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
                 cplx<T> ga, gb;
-                noise_pair_unit<T>(ks, in.seed, i0, i1a, i2a, ga, gb);
+                noise_pair_unit<T>(ks, in.seed, in.nstream, i0, i1a, i2a, ga, gb);
                 if (XS(&snoise[(j + P / 2) * S::THREADS + tid], 431)) {
                     snoise[j * S::THREADS + tid] = ga;
                     snoise[(j + P / 2) * S::THREADS + tid] = gb;

@@ -86,3 +86,49 @@ def summarise(recs, makespan, rate):
             "service_p50_s": q(serv, 50), "service_p99_s": q(serv, 99),
             "served_gpt_steps_per_s": work / span / 1e9, "makespan_s": makespan,
             "offered_gpt_steps_per_s": rate * work / len(recs) / 1e9}
+
+
+def sequential_estimate(stream, precision, k_short=20, k_long=60):
+    """Solves of `stream` run one after another in one process, each alone in
+    its own xpfc_ctx at `precision` (the plain sequential baseline of the
+    serving loop), estimated from two timed solves per grid size: a solve of
+    N^3 and k steps takes a_N + b_N k seconds (create, device initial field,
+    step with its diagnostics, read-back of the diagnostics, destroy).
+    Returns solves/s over the stream, and the latency percentiles of a FIFO
+    queue served that way under the stream's own arrival times."""
+    from .api import Xpfc
+    import ctypes as C
+    cost = {}
+    for N in sorted({p.Mx for _, p, _ in stream}):
+        p = [q for _, q, _ in stream if q.Mx == N][0]
+        q = type(p)()
+        C.pointer(q)[0] = p
+        q.precision = precision
+        t = {}
+        for k in (k_short, k_long):
+            best = None
+            for _ in range(2):
+                t0 = time.perf_counter()
+                with Xpfc(q) as x:
+                    x.initialize(None)
+                    x.step(k)
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            t[k] = best
+        b = max((t[k_long] - t[k_short]) / (k_long - k_short), 0.0)
+        cost[N] = (max(t[k_short] - b * k_short, 0.0), b)
+    service = [cost[p.Mx][0] + cost[p.Mx][1] * k for _, p, k in stream]
+    free = 0.0
+    lat = []
+    for (t_arr, _, _), s in zip(stream, service):
+        start = max(free, t_arr)
+        free = start + s
+        lat.append(free - t_arr)
+    lat = np.array(lat)
+    return {"value": len(stream) / sum(service), "unit": "solves/s",
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "total_service_s": float(sum(service)),
+            "per_size": {"%d^3" % N: {"per_solve_s": a, "per_step_ms": 1e3 * b} for N, (a, b) in cost.items()},
+            "how": "per grid size, solves of %d and %d steps timed alone (best of 2); service time = a_N + b_N steps "
+                   "summed over the stream's requests; latencies from a FIFO queue under the stream's arrivals"
+                   % (k_short, k_long)}
