@@ -160,7 +160,7 @@ def test_fused_mixed_within_tolerance(oracle_mod, shape, steps, fcc):
 @pytest.mark.parametrize("shape,steps", [((48, 48, 48), 60), ((96, 96, 96), 30), ((192, 192, 1), 60),
                                          ((48, 96, 192), 20), ((512, 512, 1), 30), ((1024, 1024, 1), 20),
                                          ((256, 2048, 1), 10), ((512, 16, 16), 20), ((16, 512, 32), 20),
-                                         ((512, 64, 1), 30)])
+                                         ((512, 64, 1), 30), ((4096, 4096, 1), 3)])
 def test_fused_mixed_radix3_sizes(oracle_mod, shape, steps):
     """The 12- and 24-point register plans (48, 96, 192) and the large 2-D
     grids on the mixed path, with conserved noise, against the FP64 oracle."""

@@ -274,10 +274,14 @@ template <typename T, int N, int NG> struct RPenShape {
     // area of their own while their global loads are in flight; the 24-value
     // plans (which park W in the transpose scratch) draw it after the
     // transforms, into the scratch of S
-    static constexpr bool EARLY_NOISE = P <= 16;
+    // (only where the staging area keeps the block within 160 KB of shared
+    // memory: the long 2-D lines of 4096 would not fit)
+    static constexpr size_t SMEM0 = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
+    static constexpr bool EARLY_NOISE =
+        P <= 16 && SMEM0 + sizeof(cplx<T>) * (size_t)P * THREADS <= (size_t)160 * 1024;
     static constexpr int NZ = EARLY_NOISE ? P * THREADS : 0;
-    static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP + (size_t)NZ) +
-                                   sizeof(double) * 32 * NQ_PEN;
+    static constexpr size_t SMEM = SMEM0 + sizeof(cplx<T>) * (size_t)NZ;
+    static_assert(SMEM <= (size_t)227 * 1024, "the pencil block must fit one SM's shared memory");
     // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
     // and bufW and writes its results after them in bufS (2 NG N values)
     static_assert(!RP<N>::ok || 2 * NG * N <= LINES * LP, "bufS must hold the slot-0 areas");
