@@ -281,7 +281,8 @@ template <typename T, int N, int NG> struct RPenShape {
         P <= 16 && SMEM0 + sizeof(cplx<T>) * (size_t)P * THREADS <= (size_t)160 * 1024;
     static constexpr int NZ = EARLY_NOISE ? P * THREADS : 0;
     static constexpr size_t SMEM = SMEM0 + sizeof(cplx<T>) * (size_t)NZ;
-    static_assert(SMEM <= (size_t)227 * 1024, "the pencil block must fit one SM's shared memory");
+    static_assert(!reg_pen_ok<T, N>() || SMEM <= (size_t)227 * 1024,
+                  "a register pencil block must fit one SM's shared memory");
     // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
     // and bufW and writes its results after them in bufS (2 NG N values)
     static_assert(!RP<N>::ok || 2 * NG * N <= LINES * LP, "bufS must hold the slot-0 areas");
