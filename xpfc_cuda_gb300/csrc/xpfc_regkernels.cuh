@@ -270,19 +270,7 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int THREADS = TX * Q * NG;
     static constexpr int LP = line_pitch<T, N, TX>();
     static constexpr int LINES = TX * NG;
-    // plans of at most 16 values per thread draw their noise into a staging
-    // area of their own while their global loads are in flight; the 24-value
-    // plans (which park W in the transpose scratch) draw it after the
-    // transforms, into the scratch of S
-    // (only where the staging area keeps the block within 160 KB of shared
-    // memory: the long 2-D lines of 4096 would not fit)
-    static constexpr size_t SMEM0 = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
-    static constexpr bool EARLY_NOISE =
-        P <= 16 && SMEM0 + sizeof(cplx<T>) * (size_t)P * THREADS <= (size_t)160 * 1024;
-    static constexpr int NZ = EARLY_NOISE ? P * THREADS : 0;
-    static constexpr size_t SMEM = SMEM0 + sizeof(cplx<T>) * (size_t)NZ;
-    static_assert(!reg_pen_ok<T, N>() || SMEM <= (size_t)227 * 1024,
-                  "a register pencil block must fit one SM's shared memory");
+    static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
     // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
     // and bufW and writes its results after them in bufS (2 NG N values)
     static_assert(!RP<N>::ok || 2 * NG * N <= LINES * LP, "bufS must hold the slot-0 areas");
@@ -355,7 +343,6 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     cplx<T> *bufS = stw + N;
     cplx<T> *bufW = bufS + S::LINES * S::LP;
     double *sred = reinterpret_cast<double *>(bufW + S::LINES * S::LP);
-    cplx<T> *snz = reinterpret_cast<cplx<T> *>(sred + 32 * NQ_PEN);   // early noise staging (NZ values)
     const int tid = threadIdx.x;
     for (int i = tid; i < N; i += S::THREADS)
         if (XG(&twN[i], 421) && XS(&stw[i], 422)) stw[i] = twN[i];
@@ -387,29 +374,6 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
         const long long e = (long long)(t + Q * j) * args.es;
         if constexpr (!STASH) vs[j] = (valid && XG(&gS[e], 423)) ? gS[e] : mk<T>((T)0, (T)0);
         vw[j] = (valid && XG(&gW[e], 424)) ? gW[e] : mk<T>((T)0, (T)0);
-    }
-    // interior columns: modes j and j + P/2 sit at kz and kz + N/2 and share
-    // one Philox draw.  The draws depend on nothing the loads bring, so the
-    // plans with a staging area of their own make them here, in a rolled loop
-    // (the Philox and Box-Muller code appears once in the instruction stream),
-    // while the loads above are in flight; each thread reads back only its
-    // own entries.
-    const bool interior = valid && kx0 + c != 0;
-    const int i0 = kx0 + c;
-    if constexpr (S::EARLY_NOISE) {
-        if (ks.noise_on && interior) {
-#pragma unroll 1
-            for (int j = 0; j < P / 2; j++) {
-                const int kza = t + Q * j;
-                const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
-                cplx<T> ga, gb;
-                noise_pair_unit<T>(ks, in.seed, in.nstream, i0, i1a, i2a, ga, gb);
-                if (XS(&snz[(j + P / 2) * S::THREADS + tid], 436)) {
-                    snz[j * S::THREADS + tid] = ga;
-                    snz[(j + P / 2) * S::THREADS + tid] = gb;
-                }
-            }
-        }
     }
     __syncthreads();
     const int ln = g * TX + c;
@@ -478,11 +442,16 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
                 if (XS(&outS[g * N + t + Q * j], 430)) vs[j] = outS[g * N + t + Q * j];
         }
     }
-    // the 24-value plans draw the interior noise now, into bufS (free
-    // between the two transforms), in the same rolled loop
-    cplx<T> *snoise = S::EARLY_NOISE ? snz : bufS;
-    static_assert(S::EARLY_NOISE || P * S::THREADS <= S::LINES * S::LP, "noise staging must fit in bufS");
-    if (!S::EARLY_NOISE && ks.noise_on) {
+    // interior columns: modes j and j + P/2 sit at kz and kz + N/2 and share
+    // one Philox draw.  The draws are made first, in a rolled loop, into
+    // shared memory (bufS is free between the two transforms; each thread
+    // reads back only its own entries), so that the Philox and Box-Muller code
+    // appears once in the instruction stream instead of P/2 times.
+    const bool interior = valid && kx0 + c != 0;
+    const int i0 = kx0 + c;
+    cplx<T> *snoise = bufS;
+    static_assert(P * S::THREADS <= S::LINES * S::LP, "noise staging must fit in bufS");
+    if (ks.noise_on) {
         __syncthreads();   // the forward transform and the slot-0 pass are done with bufS
         if (interior) {
 #pragma unroll 1
