@@ -473,12 +473,8 @@ template <bool ROLLED = true>
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 #pragma unroll(ROLLED ? 1 : 10)
     for (int r = 0; r < 10; r++) {
-        // each 32 x 32 -> 64-bit product as one wide multiply (its low and
-        // high words are the round's lo and hi)
-        const unsigned long long p0 = (unsigned long long)0xD2511F53u * c.x;
-        const unsigned long long p1 = (unsigned long long)0xCD9E8D57u * c.z;
-        const uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
-        const uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
         c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
         k.x += 0x9E3779B9u;
         k.y += 0xBB67AE85u;
