@@ -73,7 +73,7 @@ def test_batch_fp64_matches_oracle(oracle_mod):
             for r in b.collect(i):
                 it = r["iteration"]
                 if r["F"] is not None:
-                    assert abs(r["F"] - F[it]) <= 1e-11 * abs(F[it]), (i, it)
+                    assert abs(r["F"] - F[it]) <= 1e-12 * abs(F[it]), (i, it)
                 if r["rms"] is not None:
                     assert abs(r["rms"] - rms[it]) <= 1e-8 * abs(rms[it]) + 1e-14, (i, it)
 

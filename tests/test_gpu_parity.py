@@ -95,7 +95,7 @@ def test_fused_fp64_matches_oracle(oracle_mod, shape, steps):
     for r in recs:
         i = r["iteration"]
         if r["F"] is not None:
-            assert abs(r["F"] - F[i]) <= 1e-11 * abs(F[i]), (i, r["F"], F[i])
+            assert abs(r["F"] - F[i]) <= 1e-12 * abs(F[i]), (i, r["F"], F[i])
             assert abs(r["mean"] - mean[i]) <= 1e-13
         if r["rms"] is not None:
             assert abs(r["rms"] - rms[i]) <= 1e-8 * abs(rms[i]) + 1e-14, (i, r["rms"], rms[i])
@@ -116,7 +116,7 @@ def test_fused_fp64_large_2d_matches_oracle(oracle_mod, shape, steps):
     assert rel_l2(field, ref) < 1e-10
     for r in recs:
         if r["F"] is not None:
-            assert abs(r["F"] - F[r["iteration"]]) <= 1e-11 * abs(F[r["iteration"]])
+            assert abs(r["F"] - F[r["iteration"]]) <= 1e-12 * abs(F[r["iteration"]])
 
 
 def test_staged_fp64_matches_oracle(oracle_mod):
