@@ -42,9 +42,8 @@ METRIC = "Gpt-steps/s @256^3 mixed vs FP64 on 1 GB300 (F rel<=1e-6); sweep solve
 UNIT = "Gpt-steps/s"
 DX = 0.125
 FCC = ((2 * math.pi, 1.0, 1.0, 8.0), (2 * math.pi * 2 / math.sqrt(3), 1.0, 1.0, 6.0))
-# per-pass algorithmic bytes as multiples of one packed field array (N^3 elements)
+# the step's passes (algorithmic bytes per launch from xpfc_pass_bytes)
 PASS_NAMES = {0: "pencil_kernel", 1: "col_kernel(inverse)", 2: "row_kernel(fused)", 3: "col_kernel(forward)"}
-PASS_ARRAYS = {0: 3, 1: 2, 2: 2, 3: 2}
 FLOOR_BYTES_PER_POINT = 16.125   # two read+write sweeps of the FP32 state at 256^3
 SIGMA = 0.22
 
@@ -487,20 +486,20 @@ def run_ours(args):
 
     # roofline of the dominant pass
     peak, peak_kind = measured_peak()
-    esz = 4 if prec == X._lib.MIXED else 8
     passes = {k: v for k, v in prof.items() if k in PASS_NAMES and v[1] > 0}
     dom = max(passes, key=lambda k: passes[k][0]) if passes else None
     roof = None
     if dom is not None:
         avg_ms = passes[dom][0] / passes[dom][1]
-        alg = PASS_ARRAYS[dom] * esz * n ** 3
+        alg = x.pass_bytes(dom)
         achieved = alg / (avg_ms / 1e3) / 1e9
         traffic = load_traffic(PASS_NAMES[dom], n)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": PASS_NAMES[dom], "algorithmic_bytes": alg,
                 "avg_launch_ms": avg_ms, "peak_source": peak_kind,
                 "passes": {PASS_NAMES[k]: {"avg_ms": v[0] / v[1], "launches": v[1],
-                                           "GB/s": PASS_ARRAYS[k] * esz * n ** 3 / (v[0] / v[1] / 1e3) / 1e9}
+                                           "algorithmic_bytes": x.pass_bytes(k),
+                                           "GB/s": x.pass_bytes(k) / (v[0] / v[1] / 1e3) / 1e9}
                            for k, v in passes.items()},
                 "step_frac_of_two_sweep_floor": (value * 1e9 / ws) * FLOOR_BYTES_PER_POINT / (peak * 1e9)}
 

@@ -331,6 +331,11 @@ int xpfc_FE_calc_noalloc(const double *psi, const double *psi2, const double *ps
 /* ---- introspection ---------------------------------------------------------- */
 /* Kernel launches issued by this context since creation (all entry points). */
 long long xpfc_launch_count(const xpfc_ctx *ctx);
+/* Algorithmic HBM bytes of one launch of a step pass (pass ids as in
+   xpfc_get_profile: 0 pencil, 1 and 3 column passes, 2 row pass): the arrays
+   the pass reads and writes once each, for the roofline of that pass.  No
+   reference counterpart.  -1 for a bad pass id or context. */
+long long xpfc_pass_bytes(const xpfc_ctx *ctx, int pass);
 /* Library version string. */
 const char *xpfc_version(void);
 

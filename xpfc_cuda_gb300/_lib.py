@@ -140,6 +140,7 @@ SIGNATURES = [
     ("xpfc_FE_calc_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong,
                                         C.c_double, C.c_double, C.c_double, _dp, C.c_void_p]),
     ("xpfc_launch_count", C.c_longlong, [_ctx]),
+    ("xpfc_pass_bytes", C.c_longlong, [_ctx, C.c_int]),
     ("xpfc_version", C.c_char_p, []),
 ]
 

@@ -198,6 +198,10 @@ class Xpfc:
     get_field = copy2cpu
 
     # ---- staged path: the reference's per-stage wrappers ---------------------
+    def pass_bytes(self, npass):
+        """Algorithmic HBM bytes of one launch of a step pass (xpfc_pass_bytes)."""
+        return self._L.xpfc_pass_bytes(self._h, npass)
+
     def copy2cpu_async(self):
         """Starts reading the current field back (copy_to_cpu.cu:3-18) on the
         context's copy stream; steps enqueued afterwards overlap the copy.

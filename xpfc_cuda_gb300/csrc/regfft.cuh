@@ -41,7 +41,7 @@ template <> struct RP<256> { static constexpr bool ok = true, three = false; sta
 // about 400 bytes per thread).  The one-line row and column passes keep it
 // for the 32-value plan too, whose 167 registers leave one block per SM and
 // ran slower than the shared-memory kernel (594 against 405 us at 512^3).
-template <typename T, int N> constexpr bool reg_pen_ok() {
+template <typename T, int N> __host__ __device__ constexpr bool reg_pen_ok() {
     return RP<N>::ok && (sizeof(T) == 4 ? RP<N>::P <= 24 : (RP<N>::P <= 16 && RP<N>::Q <= 64));
 }
 template <typename T, int N> constexpr bool reg_line_ok() {

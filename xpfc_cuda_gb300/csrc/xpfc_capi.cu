@@ -102,6 +102,10 @@ struct xpfc_ctx {
     std::string err;
     // fused state (T = float for XPFC_MIXED, double for XPFC_FP64)
     void *S = nullptr, *W = nullptr, *X = nullptr;
+    // 3-D FP32 grids with a register pencil plan keep S's pencil-axis
+    // spectrum between steps (the pencil pass then transforms only W forward)
+    void *Shat = nullptr;
+    bool spec = false;
     size_t esz = 8;
     // twiddle tables W_L^k (k < L), keyed by (L, is_double), and the host
     // sources of their stream-ordered uploads
@@ -352,6 +356,17 @@ extern "C" void *xpfc_get_stream(const xpfc_ctx *ctx) { return ctx ? (void *)ctx
 
 extern "C" long long xpfc_launch_count(const xpfc_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+extern "C" long long xpfc_pass_bytes(const xpfc_ctx *ctx, int pass) {
+    if (!ctx) return -1;
+    const long long arr = (long long)ctx->esz * ctx->ncells * ctx->nb;   // one field array
+    switch (pass) {
+        case 0: return (ctx->spec ? 4 : 3) * arr;           // pencil: S (or Shat), W in; S (and Shat) out
+        case 1: case 3: return ctx->three_d ? 2 * arr : 0;   // column passes
+        case 2: return 2 * arr;                              // row pass
+        default: return -1;
+    }
+}
+
 extern "C" long long xpfc_iteration(const xpfc_ctx *ctx) { return ctx ? ctx->iteration : -1; }
 
 extern "C" int xpfc_build_initial_field(const xpfc_params *p, double *host_psi) {
@@ -548,6 +563,18 @@ static int check_params(const xpfc_params *q) {
     return XPFC_OK;
 }
 
+// Whether a context keeps S's pencil-axis spectrum (Shat): 3-D FP32 grids
+// whose pencil length has the kept-spectrum register pencil, unless
+// XPFC_SPEC=0 (or XPFC_TMA=1, whose staged pencil transforms S each step).
+static bool spec_for(const xpfc_params &p) {
+    static const bool on = [] {
+        const char *e = getenv("XPFC_SPEC");
+        const char *t = getenv("XPFC_TMA");
+        return !(e && e[0] == '0') && !(t && t[0] == '1');
+    }();
+    return on && p.Mz > 1 && p.precision == XPFC_MIXED && pen_spec_supported(p.Mx, 4);
+}
+
 static int create_group(const xpfc_params *ps, int nb, xpfc_ctx **out) {
     const xpfc_params *p = ps;
     for (int i = 0; i < nb; i++) {
@@ -596,6 +623,15 @@ static int create_group(const xpfc_params *ps, int nb, xpfc_ctx **out) {
     }
     poison(ctx->S, bytes, ctx->stream);
     poison(ctx->W, bytes, ctx->stream);
+    if (spec_for(*p)) {
+        if (cudaMalloc(&ctx->Shat, bytes) != cudaSuccess) {
+            set_thread_error("device allocation of the kept spectrum failed");
+            xpfc_destroy(ctx);
+            return XPFC_ENOMEM;
+        }
+        poison(ctx->Shat, bytes, ctx->stream);
+        ctx->spec = true;
+    }
     rc = build_tables(ctx);
     if (rc == XPFC_OK) {
         const int L0 = ctx->L0;
@@ -656,6 +692,7 @@ extern "C" int xpfc_destroy(xpfc_ctx *ctx) {
     cudaFree(ctx->S);
     cudaFree(ctx->W);
     cudaFree(ctx->X);
+    cudaFree(ctx->Shat);
     for (auto &kv : ctx->tw) cudaFree(kv.second);
     cudaFree(ctx->table_f);
     cudaFree(ctx->table_d);
@@ -810,6 +847,22 @@ static int init_fused(xpfc_ctx *ctx, const double *dpsi) {
     if (ctx->three_d) {
         rc = fft_forward_xy<T>(ctx, ctx->W, false);
         if (rc != XPFC_OK) return rc;
+    }
+    if (ctx->spec) {
+        // the kept spectrum: S transformed forward along the pencil axis (the
+        // n1 L0 columns of every plane are contiguous, planes n1 L0 apart)
+        void *twz = twiddle(ctx, ctx->n2, dbl);
+        if (!twz) return fail(ctx, XPFC_ENOMEM, "twiddle tables");
+        ColArgs cz{};
+        cz.in = ctx->S;
+        cz.out = ctx->Shat;
+        cz.es = (long long)ctx->n1 * ctx->L0;
+        cz.ostride = 0;
+        cz.scale = 1.0;
+        cz.ncols = (long long)ctx->n1 * ctx->L0;
+        cz.zstride = ctx->zstride;
+        cz.nz = ctx->nb;
+        XPFC_LAUNCH(ctx, launch_col<T>(-1, ctx->n2, cz, 1, twz, ctx->stream));
     }
     return XPFC_OK;
 }
@@ -1001,6 +1054,7 @@ static int launch_pencil_pass(xpfc_ctx *ctx, long long step, int update, int wan
     PenArgs pa{};
     pa.S = ctx->S;
     pa.W = ctx->W;
+    pa.Shat = ctx->spec ? ctx->Shat : nullptr;
     pa.es = ctx->three_d ? (long long)ctx->n1 * ctx->L0 : ctx->L0;
     pa.gstride = ctx->three_d ? ctx->L0 : 0;
     pa.three_d = ctx->three_d;
@@ -1693,7 +1747,7 @@ extern "C" int xpfc_get_field_wait(xpfc_ctx *ctx, double *host_psi, long long *i
 namespace {
 struct SnapHeader {
     char magic[8];            // "XPFCSNP1"
-    int32_t esz, nb, Mx, My, Mz, pad;
+    int32_t esz, nb, Mx, My, Mz, narrays;   // S, W (and the kept spectrum)
     int64_t iteration;
     int64_t bytes;            // bytes of S (and of W)
     double psi0;
@@ -1705,11 +1759,14 @@ extern "C" int xpfc_save_state(xpfc_ctx *ctx, const char *path) {
     if (!ctx->initialized) return fail(ctx, XPFC_ESTATE, "no state before xpfc_initialize");
     XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
     const size_t bytes = ctx->esz * (size_t)ctx->ncells * ctx->nb;
-    int rc = host_stage(ctx, 2 * bytes);
+    const int narr = ctx->spec ? 3 : 2;
+    int rc = host_stage(ctx, narr * bytes);
     if (rc != XPFC_OK) return rc;
     char *h = static_cast<char *>(ctx->hstage);
     XPFC_CUDA(ctx, cudaMemcpyAsync(h, ctx->S, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     XPFC_CUDA(ctx, cudaMemcpyAsync(h + bytes, ctx->W, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->spec)
+        XPFC_CUDA(ctx, cudaMemcpyAsync(h + 2 * bytes, ctx->Shat, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     SnapHeader hd{};
     memcpy(hd.magic, "XPFCSNP1", 8);
@@ -1720,10 +1777,11 @@ extern "C" int xpfc_save_state(xpfc_ctx *ctx, const char *path) {
     hd.Mz = ctx->p.Mz;
     hd.iteration = ctx->iteration;
     hd.bytes = (int64_t)bytes;
+    hd.narrays = narr;
     hd.psi0 = ctx->p.psi0;
     FILE *f = fopen(path, "wb");
     if (!f) return fail(ctx, XPFC_EIO, std::string("cannot open ") + path);
-    const bool ok = fwrite(&hd, sizeof(hd), 1, f) == 1 && fwrite(h, 1, 2 * bytes, f) == 2 * bytes;
+    const bool ok = fwrite(&hd, sizeof(hd), 1, f) == 1 && fwrite(h, 1, narr * bytes, f) == narr * bytes;
     if (fclose(f) != 0 || !ok) return fail(ctx, XPFC_EIO, std::string("write failed: ") + path);
     return XPFC_OK;
 }
@@ -1739,12 +1797,13 @@ extern "C" int xpfc_load_state(xpfc_ctx *ctx, const char *path) {
         fclose(f);
         return fail(ctx, XPFC_EIO, std::string("not a state snapshot: ") + path);
     }
+    const int narr = ctx->spec ? 3 : 2;
     if (hd.esz != (int32_t)ctx->esz || hd.nb != ctx->nb || hd.Mx != ctx->p.Mx || hd.My != ctx->p.My ||
-        hd.Mz != ctx->p.Mz || hd.bytes != (int64_t)bytes) {
+        hd.Mz != ctx->p.Mz || hd.bytes != (int64_t)bytes || hd.narrays != narr) {
         fclose(f);
         return fail(ctx, XPFC_EINVAL, "the snapshot's grid, precision or instance count differs from the context's");
     }
-    int rc = host_stage(ctx, 2 * bytes);
+    int rc = host_stage(ctx, narr * bytes);
     if (rc != XPFC_OK) {
         fclose(f);
         return rc;
@@ -1752,11 +1811,13 @@ extern "C" int xpfc_load_state(xpfc_ctx *ctx, const char *path) {
     char *h = static_cast<char *>(ctx->hstage);
     // the staging buffer may still feed an upload enqueued earlier
     XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    const bool ok = fread(h, 1, 2 * bytes, f) == 2 * bytes;
+    const bool ok = fread(h, 1, narr * bytes, f) == narr * bytes;
     fclose(f);
     if (!ok) return fail(ctx, XPFC_EIO, std::string("truncated snapshot: ") + path);
     XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->S, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
     XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->W, h + bytes, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (ctx->spec)
+        XPFC_CUDA(ctx, cudaMemcpyAsync(ctx->Shat, h + 2 * bytes, bytes, cudaMemcpyHostToDevice, ctx->stream));
     XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->iteration = hd.iteration;
     ctx->initialized = true;

@@ -537,6 +537,7 @@ __device__ __forceinline__ void noise_pair_unit(const KSpace &ks, unsigned long 
 struct PenArgs {
     void *S;
     const void *W;
+    void *Shat;          // kept pencil-axis spectrum of S (null: transform S each step)
     long long es;        // pencil element stride (complex)
     long long gstride;   // stride of the paired axis (3-D: L0), 0 in 2-D
     int three_d;

@@ -33,6 +33,9 @@ cudaError_t launch_pencil(int L, int ng, const PenArgs &a, const KSpace &ks, int
 // for that length and element size); the pass needs L0 % tx == 0.  err: a
 // device word that a block which gave up waiting sets to XPFC_DEV_ETIMEDOUT.
 int pen_tma_tx(int L, int esz);
+// Whether a 3-D pencil length has the kept-spectrum register pencil
+// (PenArgs::Shat; FP32 only).
+bool pen_spec_supported(int L, int esz);
 template <typename T>
 cudaError_t launch_pencil_tma(int L, const PenArgs &a, const KSpace &ks, int npairs, const void *twL,
                               const CUtensorMap *mapS, const CUtensorMap *mapW, int *err, cudaStream_t s,

@@ -331,9 +331,23 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const Inst &in,
     return xn;
 }
 
-template <typename T, int N, int NG, bool RED>
+// SPEC (args.Shat set): the pencil-axis spectrum of S is kept from one step
+// to the next in its own array (Shat), so the pass reads Shat instead of
+// transforming S forward, and writes the updated spectrum to Shat beside the
+// inverse-transformed S that the xy passes read: one array more of HBM
+// traffic (read and written) for one transform less (of three) in an
+// issue-bound pass.  The 3-D slot-0 pass needs room for its unscaled results
+// too (3 NG N values in bufS).
+// (the 24-value plans, which park W in the scratch, spilled with it)
+template <typename T, int N, int NG> __host__ __device__ constexpr bool spec_ok() {
+    return reg_pen_ok<T, N>() && RP<N>::P <= 16 && NG == 2 &&
+           3 * NG * N <= RPenShape<T, N, NG>::LINES * RPenShape<T, N, NG>::LP;
+}
+
+template <typename T, int N, int NG, bool RED, bool SPEC = false>
 __global__ void __launch_bounds__(RPenShape<T, N, NG>::THREADS, RPenShape<T, N, NG>::MINB)
 pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
+    static_assert(!SPEC || spec_ok<T, N, NG>(), "no room for the kept spectrum's slot-0 results");
     Inst in = inst_of<T>(ks);
     in.pin = pin_of(args);
     using S = RPenShape<T, N, NG>;
@@ -358,6 +372,9 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     const long long off = (long long)blockIdx.z * args.zstride + (long long)yg * args.gstride + kx0 + c;
     cplx<T> *gS = reinterpret_cast<cplx<T> *>(args.S) + off;
     const cplx<T> *gW = reinterpret_cast<const cplx<T> *>(args.W) + off;
+    // SPEC: the state is read from (and its update written to) the kept
+    // spectrum instead
+    cplx<T> *gH = SPEC ? reinterpret_cast<cplx<T> *>(args.Shat) + off : gS;
     // Plans of 24 values per thread would hold 48 values of S and W through
     // both transforms (over 255 registers, with spills).  They load and
     // transform W first and keep it in its line's scratch of bufW, in natural
@@ -372,7 +389,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
 #pragma unroll
     for (int j = 0; j < P; j++) {
         const long long e = (long long)(t + Q * j) * args.es;
-        if constexpr (!STASH) vs[j] = (valid && XG(&gS[e], 423)) ? gS[e] : mk<T>((T)0, (T)0);
+        if constexpr (!STASH) vs[j] = (valid && XG(&gH[e], 423)) ? gH[e] : mk<T>((T)0, (T)0);
         vw[j] = (valid && XG(&gW[e], 424)) ? gW[e] : mk<T>((T)0, (T)0);
     }
     __syncthreads();
@@ -386,12 +403,15 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
 #pragma unroll
         for (int j = 0; j < P; j++) {
             const long long e = (long long)(t + Q * j) * args.es;
-            vs[j] = (valid && XG(&gS[e], 423)) ? gS[e] : mk<T>((T)0, (T)0);
+            vs[j] = (valid && XG(&gH[e], 423)) ? gH[e] : mk<T>((T)0, (T)0);
         }
-        reg_fft<T, N, -1>(vs, t, bufS + ln * S::LP, stw);
+        if constexpr (!SPEC) reg_fft<T, N, -1>(vs, t, bufS + ln * S::LP, stw);
+    } else if constexpr (SPEC) {
+        reg_fft<T, N, -1>(vw, t, bufW + ln * S::LP, stw);
     } else {
         reg_fft2<T, N, -1>(vs, vw, t, bufS + ln * S::LP, bufW + ln * S::LP, stw);
     }
+    const bool keep = SPEC && args.update;   // write the updated spectrum to Shat
 
     DSum<T, NQ_PEN> acc;
     const T sc = (T)args.scale;
@@ -407,6 +427,7 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     // holds them (group gg at gg WG).
     if (kx0 == 0) {
         cplx<T> *outS = bufS + G * N;                  // after the [group][kz] publish area of S
+        cplx<T> *outU = bufS + 2 * G * N;              // SPEC: the unscaled results, for Shat
         __syncthreads();
         if (c == 0 && g < G) {
 #pragma unroll
@@ -433,13 +454,21 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
             const cplx<T> x0 = update_mode<T>(ks, in, args, 0, i1, i2, s0, w0, acc, (T)1);
             const cplx<T> xN = update_mode<T>(ks, in, args, nh, i1, i2, sN, wN, acc, (T)1);
-            outS[gg * N + kz] = cscale(cadd(x0, cmuli<1>(xN)), sc);
+            const cplx<T> packed = cadd(x0, cmuli<1>(xN));
+            outS[gg * N + kz] = cscale(packed, sc);
+            if constexpr (SPEC)
+                if (XS(&outU[gg * N + kz], 437)) outU[gg * N + kz] = packed;
         }
         __syncthreads();
         if (c == 0 && g < G) {
 #pragma unroll
-            for (int j = 0; j < P; j++)
+            for (int j = 0; j < P; j++) {
                 if (XS(&outS[g * N + t + Q * j], 430)) vs[j] = outS[g * N + t + Q * j];
+                if constexpr (SPEC) {
+                    const long long e = (long long)(t + Q * j) * args.es;
+                    if (keep && XS(&outU[g * N + t + Q * j], 438) && XG(&gH[e], 439)) gH[e] = outU[g * N + t + Q * j];
+                }
+            }
         }
     }
     // interior columns: modes j and j + P/2 sit at kz and kz + N/2 and share
@@ -484,8 +513,16 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
                 wa = XS(&bufW[ln * S::LP + kza], 434) ? bufW[ln * S::LP + kza] : zero;
                 wb = XS(&bufW[ln * S::LP + kzb], 435) ? bufW[ln * S::LP + kzb] : zero;
             }
-            vs[j] = cscale(update_coef<T, RED>(ks, ca, vs[j], wa, na, acc, (T)2), sc);
-            vs[j + P / 2] = cscale(update_coef<T, RED>(ks, cb, vs[j + P / 2], wb, nb, acc, (T)2), sc);
+            const cplx<T> xa = update_coef<T, RED>(ks, ca, vs[j], wa, na, acc, (T)2);
+            const cplx<T> xb = update_coef<T, RED>(ks, cb, vs[j + P / 2], wb, nb, acc, (T)2);
+            if constexpr (SPEC) {
+                if (keep && XG(&gH[(long long)kza * args.es], 440) && XG(&gH[(long long)kzb * args.es], 441)) {
+                    gH[(long long)kza * args.es] = xa;
+                    gH[(long long)kzb * args.es] = xb;
+                }
+            }
+            vs[j] = cscale(xa, sc);
+            vs[j + P / 2] = cscale(xb, sc);
         }
     }
     if (RED) {
