@@ -338,9 +338,12 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const Inst &in,
 // traffic (read and written) for one transform less (of three) in an
 // issue-bound pass.  The 3-D slot-0 pass needs room for its unscaled results
 // too (3 NG N values in bufS).
-// (the 24-value plans, which park W in the scratch, spilled with it)
+// Measured on GB300 (pencil per launch): 256^3 116 against 120 us (step
+// 0.174 against 0.176 ms), 128^3 41.2 against 40.0 us, 64^3 no change; the
+// 24-value plans, which park W in the scratch, spilled with it.  So lines of
+// 256 and more only.
 template <typename T, int N, int NG> __host__ __device__ constexpr bool spec_ok() {
-    return reg_pen_ok<T, N>() && RP<N>::P <= 16 && NG == 2 &&
+    return reg_pen_ok<T, N>() && RP<N>::P <= 16 && N >= 256 && NG == 2 &&
            3 * NG * N <= RPenShape<T, N, NG>::LINES * RPenShape<T, N, NG>::LP;
 }
 
