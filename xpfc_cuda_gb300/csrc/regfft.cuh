@@ -112,9 +112,17 @@ __device__ __forceinline__ void reg_fft3(cplx<T> *v, int t, cplx<T> *buf, const 
 
 // v: P registers (element t + Q j).  buf: this line's scratch.  tw: W_N^k.
 // Every thread of the block must call it (two __syncthreads inside, four
-// for the three-level plans).
-template <typename T, int N, int DIR>
+// for the three-level plans).  WARP: the Q threads of every line sit in one
+// warp and the scratch is the line's own (the row pass), so the transposes
+// only need the warp to agree (__syncwarp) instead of the whole block.
+template <bool WARP> __device__ __forceinline__ void line_sync() {
+    if constexpr (WARP) __syncwarp();
+    else __syncthreads();
+}
+
+template <typename T, int N, int DIR, bool WARP = false>
 __device__ __forceinline__ void reg_fft(cplx<T> *v, int t, cplx<T> *buf, const cplx<T> *__restrict__ tw) {
+    static_assert(!WARP || (!RP<N>::three && RP<N>::Q <= 32), "a warp-synchronised line fits one warp");
     if constexpr (RP<N>::three) {
         reg_fft3<T, N, DIR>(v, t, buf, tw);
     } else {
@@ -123,11 +131,11 @@ __device__ __forceinline__ void reg_fft(cplx<T> *v, int t, cplx<T> *buf, const c
         dftR<P, DIR, T>(v);
 #pragma unroll
         for (int c = 1; c < P; c++) v[c] = twmul<DIR>(v[c], XS(&tw[t * c], 207) ? tw[t * c] : mk<T>((T)1, (T)0));
-        __syncthreads();
+        line_sync<WARP>();
 #pragma unroll
         for (int c = 0; c < P; c++)
             if (XS(&buf[c * QP + t], 201)) buf[c * QP + t] = v[c];
-        __syncthreads();
+        line_sync<WARP>();
         cplx<T> u[P];
 #pragma unroll
         for (int m = 0; m < M; m++)

@@ -205,7 +205,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
 
     if (MODE == ROW_INV || MODE == ROW_FUSED) {
         reg_unpack<T, N>(v, t, lane, stw2);
-        reg_fft<T, N, +1>(v, t, line, stw);
+        reg_fft<T, N, +1, true>(v, t, line, stw);
     }
     if (MODE == ROW_INV) {
         const T sc = (T)args.scale;
@@ -244,7 +244,7 @@ row_kernel_reg(RowArgs args, const cplx<T> *__restrict__ twN, const cplx<T> *__r
         }
     }
     if (MODE != ROW_INV) {
-        reg_fft<T, N, -1>(v, t, line, stw);
+        reg_fft<T, N, -1, true>(v, t, line, stw);
         reg_pack<T, N>(v, t, lane, stw2);
     }
     if (!valid) return;
