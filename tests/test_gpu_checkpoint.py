@@ -28,7 +28,9 @@ def _params(X, N, precision, two_d=False):
                             envelope=X._lib.ENVELOPE_MAX, ff_factor=DX ** 3, noise_amp=0.01, noise_seed=9)
 
 
-@pytest.mark.parametrize("N,prec,two_d", [(64, "MIXED", False), (32, "FP64", False), (128, "MIXED", True)])
+# 256^3 mixed keeps the pencil-axis spectrum of S, a third array in the snapshot
+@pytest.mark.parametrize("N,prec,two_d", [(64, "MIXED", False), (32, "FP64", False), (128, "MIXED", True),
+                                          (256, "MIXED", False)])
 def test_snapshot_resumes_bit_for_bit(tmp_path, N, prec, two_d):
     import xpfc_cuda_gb300 as X
     p = _params(X, N, getattr(X._lib, prec), two_d)

@@ -339,11 +339,14 @@ __device__ __forceinline__ cplx<T> update_mode(const KSpace &ks, const Inst &in,
 // issue-bound pass.  The 3-D slot-0 pass needs room for its unscaled results
 // too (3 NG N values in bufS).
 // Measured on GB300 (pencil per launch): 256^3 116 against 120 us (step
-// 0.174 against 0.176 ms), 128^3 41.2 against 40.0 us, 64^3 no change; the
-// 24-value plans, which park W in the scratch, spilled with it.  So lines of
-// 256 and more only.
+// 0.174 against 0.176 ms), 128^3 41.2 against 40.0 us, 512^3 1.212 against
+// 1.181 ms, 64^3 no change; the 24-value plans, which park W in the scratch,
+// spilled with it.  So lines of 256 only.  (Copying the spectrum into bufS
+// with cp.async instead, which frees its registers through W's transform and
+// keeps three blocks per SM resident at 80 registers, was slower: 130 against
+// 120 us at 256^3.)
 template <typename T, int N, int NG> __host__ __device__ constexpr bool spec_ok() {
-    return reg_pen_ok<T, N>() && RP<N>::P <= 16 && N >= 256 && NG == 2 &&
+    return reg_pen_ok<T, N>() && RP<N>::P <= 16 && N == 256 && NG == 2 &&
            3 * NG * N <= RPenShape<T, N, NG>::LINES * RPenShape<T, N, NG>::LP;
 }
 
