@@ -465,6 +465,19 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NQ], double *__re
 }
 
 // ---------------------------------------------------------------------------
+// 16-byte asynchronous global -> shared copy (cp.async, L2 only): it lands
+// without holding registers; a block's threads see it after each copying
+// thread's cp_async_wait_all and a barrier.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(sdst)),
+                 "l"(gsrc)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and Box-Muller.
 // ---------------------------------------------------------------------------
 // ROLLED keeps the round loop as a loop: code on rare paths stays small

@@ -270,7 +270,7 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int THREADS = TX * Q * NG;
     static constexpr int LP = line_pitch<T, N, TX>();
     static constexpr int LINES = TX * NG;
-    static constexpr size_t SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
+    static constexpr size_t BASE_SMEM = sizeof(cplx<T>) * (N + 2 * (size_t)LINES * LP) + sizeof(double) * 32 * NQ_PEN;
     // the slot-0 pass publishes the [group][kz] pencils at the start of bufS
     // and bufW and writes its results after them in bufS (2 NG N values)
     static_assert(!RP<N>::ok || 2 * NG * N <= LINES * LP, "bufS must hold the slot-0 areas");
@@ -279,7 +279,36 @@ template <typename T, int N, int NG> struct RPenShape {
     static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2
                                 : (sizeof(T) == 4 && P > 16)                  ? 3
                                                                               : 1;
+    // FP32 shell tables: the coefficients of the block's TX columns for every
+    // shell along the pencil (|kz| = 0 .. N/2: the two mirror rows of a block
+    // share them, and so do kz and N - kz) are staged in shared memory after
+    // the block sums, CP entries per column (odd, so that the 16-byte reads
+    // of a quarter-warp's columns are conflict-free), where that keeps MINB
+    // blocks resident per SM (228 KB, 1 KB reserved per block)
+    static constexpr int CP = N / 2 + 1;
+    static constexpr size_t CSMEM = (size_t)TX * CP * 16;
+    static constexpr bool CSM = sizeof(T) == 4 && N <= 512 && (BASE_SMEM + CSMEM + 1024) * MINB <= 233472;
+    static constexpr size_t SMEM = BASE_SMEM + (CSM ? CSMEM : 0);
+    static_assert(BASE_SMEM % 16 == 0, "the staged coefficients need 16-byte alignment");
 };
+
+// Coefficients of mode (i0, kz of the pencil): from the block's staged
+// shell entries when there are some (column c of the block), else from the
+// table in global memory or computed (kcoef).
+template <typename T, int N>
+__device__ __forceinline__ Coef<T> pen_coef(const KSpace &ks, const void *table, const float4 *scoef, int c, int i0,
+                                            int i1, int i2, int kz) {
+    if constexpr (sizeof(T) == 4) {
+        if (scoef) {
+            const int s = kz <= N / 2 ? kz : N - kz;
+            const float4 e = XS(&scoef[c * (N / 2 + 1) + s], 449) ? scoef[c * (N / 2 + 1) + s] : make_float4(0.f, 0.f, 0.f, 0.f);
+            Coef<T> r;
+            r.A = e.x; r.B = e.y; r.c2 = e.z; r.k2 = e.w;
+            return r;
+        }
+    }
+    return kcoef<T>(ks, table, i0, i1, i2);
+}
 
 // k-space sums of one updated mode: weight c2 |X|^2 (free energy) and
 // weight |res|^2 (sse_calculation.cu:133-140).  On the FP32 path, with
@@ -366,6 +395,26 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     const int tid = threadIdx.x;
     for (int i = tid; i < N; i += S::THREADS)
         if (XG(&twN[i], 421) && XS(&stw[i], 422)) stw[i] = twN[i];
+    // the shell coefficients of the block's columns, copied before the wait
+    // on the previous pass (the tables do not change during a solve), so
+    // that the update reads shared memory instead of one scattered L2 line
+    // per mode; row |s1| of the block in 3-D (both mirror rows), 0 in 2-D
+    const float4 *scoef = nullptr;
+    if constexpr (S::CSM) {
+        if (in.table) {
+            float4 *sc = reinterpret_cast<float4 *>(sred + 32 * NQ_PEN);
+            const float4 *tab = reinterpret_cast<const float4 *>(in.table);
+            const int s1 = args.three_d ? signed_idx((int)blockIdx.y, ks.n1) : 0;
+            const int kxb = blockIdx.x * TX;
+            for (int e = tid; e < TX * S::CP; e += S::THREADS) {
+                const int cc = e / S::CP, sz = e - cc * S::CP, ix = kxb + cc;
+                const int m = ix * ix + s1 * s1 + sz * sz;
+                if (ix < args.L0 && XS(&sc[e], 447) && XG(&tab[m], 448)) cp_async16(&sc[e], &tab[m]);
+            }
+            cp_async_commit();
+            scoef = sc;
+        }
+    }
     pdl_wait();
 
     const int c = tid % TX, t = (tid / TX) % Q, g = tid / (TX * Q);
@@ -399,6 +448,9 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
         vw[j] = (valid && XG(&gW[e], 424)) ? gW[e] : mk<T>((T)0, (T)0);
     }
     __syncthreads();
+    // this thread's coefficient copies are complete; the transform's first
+    // barrier publishes every thread's
+    if constexpr (S::CSM) cp_async_wait_all();
     const int ln = g * TX + c;
     if constexpr (STASH) {
         reg_fft<T, N, -1>(vw, t, bufW + ln * S::LP, stw);
@@ -508,7 +560,8 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
             const int kza = t + Q * j, kzb = kza + N / 2;
             const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
             const int i1b = args.three_d ? yg : kzb, i2b = args.three_d ? kzb : 0;
-            const Coef<T> ca = kcoef<T>(ks, in.table, i0, i1a, i2a), cb = kcoef<T>(ks, in.table, i0, i1b, i2b);
+            const Coef<T> ca = pen_coef<T, N>(ks, in.table, scoef, c, i0, i1a, i2a, kza);
+            const Coef<T> cb = pen_coef<T, N>(ks, in.table, scoef, c, i0, i1b, i2b, kzb);
             cplx<T> na = zero, nb = zero;
             if (ks.noise_on) {
                 na = cscale(snoise[j * S::THREADS + tid], noise_amp_of<T>(ks, ca.k2));
