@@ -465,12 +465,18 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NQ], double *__re
 }
 
 // ---------------------------------------------------------------------------
-// 16-byte asynchronous global -> shared copy (cp.async, L2 only): it lands
-// without holding registers; a block's threads see it after each copying
-// thread's cp_async_wait_all and a barrier.
+// Asynchronous global -> shared copies (cp.async): they land without holding
+// registers; a block's threads see them after each copying thread's
+// cp_async_wait_all and a barrier.  16 bytes (L2 only) or 8 (through L1).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(sdst)),
+                 "l"(gsrc)
+                 : "memory");
+}
+// 8-byte copy (cp.async through L1: the size that .cg does not take)
+__device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(sdst)),
                  "l"(gsrc)
                  : "memory");
 }

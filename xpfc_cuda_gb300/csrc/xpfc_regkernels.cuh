@@ -276,7 +276,12 @@ template <typename T, int N, int NG> struct RPenShape {
     static_assert(!RP<N>::ok || 2 * NG * N <= LINES * LP, "bufS must hold the slot-0 areas");
     // two resident blocks per SM (128 registers per thread) for the FP32
     // instances of 256 threads; three (168 registers) for the 24-value lines
-    static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2
+    // (four for the 128-thread FP32 blocks of 64 and 128, capped at 128
+    // registers: 128^3 56.9 -> 59.1 Gpt-steps/s against 166 registers and
+    // three blocks)
+    static constexpr int MINB = (sizeof(T) == 4 && THREADS == 64 && P <= 16)    ? 8
+                                : (sizeof(T) == 4 && THREADS == 128 && P <= 16) ? 4
+                                : (sizeof(T) == 4 && THREADS == 256 && P <= 16) ? 2
                                 : (sizeof(T) == 4 && P > 16)                  ? 3
                                                                               : 1;
     // FP32 shell tables: the coefficients of the block's TX columns for every
@@ -541,8 +546,10 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
     if (ks.noise_on) {
         __syncthreads();   // the forward transform and the slot-0 pass are done with bufS
         if (interior) {
-#pragma unroll 1
-            for (int j = 0; j < P / 2; j++) {
+            // two draws per trip (two independent Philox chains in flight:
+            // 256^3 pencil 104.6 -> 103.3 us against one per trip), one for
+            // the 24-value plans, whose registers are spent
+            auto draw = [&](int j) {
                 const int kza = t + Q * j;
                 const int i1a = args.three_d ? yg : kza, i2a = args.three_d ? kza : 0;
                 cplx<T> ga, gb;
@@ -551,6 +558,13 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
                     snoise[j * S::THREADS + tid] = ga;
                     snoise[(j + P / 2) * S::THREADS + tid] = gb;
                 }
+            };
+            if constexpr (P <= 16) {
+#pragma unroll 2
+                for (int j = 0; j < P / 2; j++) draw(j);
+            } else {
+#pragma unroll 1
+                for (int j = 0; j < P / 2; j++) draw(j);
             }
         }
     }
@@ -600,6 +614,228 @@ pencil_kernel_reg(PenArgs args, KSpace ks, const cplx<T> *__restrict__ twN) {
 #pragma unroll
     for (int j = 0; j < P; j++, o += step)
         if (XG(o, 432)) *o = vs[j];
+}
+
+// ---------------------------------------------------------------------------
+// Persistent kept-spectrum pencil (FP32, the two mirror rows of pencil_kernel_reg
+// per tile).  Each block loops over tiles: while one tile is transformed and
+// updated, W of the block's next tile is copied into a stage (cp.async, each
+// thread its own elements, so the stage needs no barrier of its own) and the
+// next tile's shell coefficients into the other half of a double buffer, so
+// that only a block's first tile waits for W.  The kept spectrum of a tile is
+// loaded into registers at its start and is first needed after W's
+// transform.  One transpose scratch serves W's forward transform, the slot-0
+// areas, the noise staging and S's inverse transform in turn.  Per mode the
+// arithmetic is pencil_kernel_reg's; the block sums go to the slot of the tile
+// (the same layout as one block per tile).
+// ---------------------------------------------------------------------------
+template <int N> struct PPenShape {
+    using R = RPenShape<float, N, 2>;
+    static constexpr int TX = R::TX, Q = R::Q, P = R::P, THREADS = R::THREADS, LINES = R::LINES, LP = R::LP;
+    static constexpr int CP = R::CP;
+    static constexpr size_t SCR = (size_t)LINES * LP;       // complex slots
+    static constexpr size_t STAGE = (size_t)P * THREADS;    // complex slots
+    static constexpr size_t OFF_SCR = sizeof(cplx<float>) * N;
+    static constexpr size_t OFF_STAGE = OFF_SCR + sizeof(cplx<float>) * SCR;
+    static constexpr size_t OFF_RED = OFF_STAGE + sizeof(cplx<float>) * STAGE;
+    static constexpr size_t OFF_COEF = OFF_RED + sizeof(double) * 32 * NQ_PEN;
+    static constexpr size_t SMEM = OFF_COEF + 2 * (size_t)TX * CP * sizeof(float4);
+    static_assert(OFF_COEF % 16 == 0, "16-byte coefficient copies");
+    // the scratch holds a line's transpose, the slot-0 areas (published S
+    // and W pencils of both rows and the results: 6 N) and the noise staging
+    static_assert(6 * N <= SCR && STAGE <= SCR, "scratch areas");
+    static_assert(2 * (SMEM + 1024) <= 233472, "two blocks per SM");
+};
+
+template <int N, bool RED>
+__global__ void __launch_bounds__(PPenShape<N>::THREADS, 2)
+pencil_kernel_pst(PenArgs args, KSpace ks, const cplx<float> *__restrict__ twN, int nkx, int npairs, int ntiles) {
+    using T = float;
+    using S = PPenShape<N>;
+    constexpr int TX = S::TX, Q = S::Q, P = S::P, THREADS = S::THREADS, CP = S::CP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *stw = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *scr = reinterpret_cast<cplx<T> *>(smem_raw + S::OFF_SCR);
+    cplx<T> *stage = reinterpret_cast<cplx<T> *>(smem_raw + S::OFF_STAGE);
+    double *sred = reinterpret_cast<double *>(smem_raw + S::OFF_RED);
+    float4 *coefs = reinterpret_cast<float4 *>(smem_raw + S::OFF_COEF);
+    const int tid = threadIdx.x;
+    const int c = tid % TX, t = (tid / TX) % Q, g = tid / (TX * Q);
+    const int ln = g * TX + c;
+    const cplx<T> zero = mk<T>((T)0, (T)0);
+    for (int i = tid; i < N; i += THREADS)
+        if (XG(&twN[i], 451) && XS(&stw[i], 452)) stw[i] = twN[i];
+
+    // this thread's share of tile tt's shell coefficients, into buffer dst
+    auto coef_copy = [&](int tt, float4 *dst) {
+        const int kx0 = (tt % nkx) * TX, rest = tt / nkx, pp = rest % npairs;
+        const float4 *tab = reinterpret_cast<const float4 *>(inst_at<T>(ks, rest / npairs).table);
+        if (!tab) return;
+        const int s1 = signed_idx(pp, ks.n1);
+        for (int e = tid; e < TX * CP; e += THREADS) {
+            const int cc = e / CP, sz = e - cc * CP, ix = kx0 + cc;
+            const int m = ix * ix + s1 * s1 + sz * sz;
+            if (ix < args.L0 && XS(&dst[e], 453) && XG(&tab[m], 454)) cp_async16(&dst[e], &tab[m]);
+        }
+    };
+    // this thread's elements of W of tile tt, into its own stage slots
+    auto w_copy = [&](int tt) {
+        const int kx0 = (tt % nkx) * TX, rest = tt / nkx, pp = rest % npairs, zi = rest / npairs;
+        const int yy1 = pp, yy2 = (ks.n1 - pp) % ks.n1;
+        const bool ok = (g == 0 || yy2 != yy1) && (kx0 + c < args.L0);
+        const cplx<T> *gw = reinterpret_cast<const cplx<T> *>(args.W) + (long long)zi * args.zstride +
+                            (long long)(g == 0 ? yy1 : yy2) * args.gstride + kx0 + c;
+#pragma unroll
+        for (int j = 0; j < P; j++) {
+            cplx<T> *d = &stage[j * THREADS + tid];
+            const long long e = (long long)(t + Q * j) * args.es;
+            if (!XS(d, 455)) continue;
+            if (ok && XG(&gw[e], 456)) cp_async8(d, &gw[e]);
+            else *d = zero;
+        }
+    };
+
+    int tile = blockIdx.x;
+    if (tile < ntiles) coef_copy(tile, coefs);   // the tables do not change during a solve
+    pdl_wait();
+    if (tile < ntiles) w_copy(tile);
+    cp_async_commit();
+    int buf = 0;
+    for (; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+        const int kxb = tile % nkx, rest = tile / nkx, p = rest % npairs, zi = rest / npairs;
+        const int y1 = p, y2 = (ks.n1 - p) % ks.n1;
+        const int G = (y2 != y1) ? 2 : 1;
+        const int yg = (g == 0) ? y1 : y2;
+        const int kx0 = kxb * TX;
+        const bool valid = (g < G) && (kx0 + c < args.L0);
+        Inst in = inst_at<T>(ks, zi);
+        in.pin = args.pin_values ? args.pin_values[zi] : args.pin_value;
+        const long long off = (long long)zi * args.zstride + (long long)yg * args.gstride + kx0 + c;
+        cplx<T> *gH = reinterpret_cast<cplx<T> *>(args.Shat) + off;
+        const float4 *scoef = in.table ? coefs + buf * TX * CP : nullptr;
+
+        // W and the coefficients of this tile have landed (every thread's
+        // copies, after the barrier), and every thread is done with the last tile
+        cp_async_wait_all();
+        __syncthreads();
+        cplx<T> vs[P], vw[P];
+#pragma unroll
+        for (int j = 0; j < P; j++) vw[j] = XS(&stage[j * THREADS + tid], 457) ? stage[j * THREADS + tid] : zero;
+        const int nt = tile + (int)gridDim.x;
+        if (nt < ntiles) {
+            w_copy(nt);
+            coef_copy(nt, coefs + (buf ^ 1) * TX * CP);
+        }
+        cp_async_commit();
+#pragma unroll
+        for (int j = 0; j < P; j++) {
+            const long long e = (long long)(t + Q * j) * args.es;
+            vs[j] = (valid && XG(&gH[e], 458)) ? gH[e] : zero;
+        }
+        reg_fft<T, N, -1>(vw, t, scr + ln * S::LP, stw);
+        const bool keep = args.update;   // write the updated spectrum to Shat
+        DSum<T, NQ_PEN> acc;
+        const T sc = (T)args.scale;
+        const int nh = args.L0;
+
+        // slot 0 (tiles holding kx' = 0), as pencil_kernel_reg: published S
+        // and W pencils of both rows, the results for the kx = 0 threads, the
+        // unscaled results straight to Shat
+        if (kx0 == 0) {
+            cplx<T> *pubS = scr, *pubW = scr + 2 * N, *outS = scr + 4 * N;
+            __syncthreads();
+            if (c == 0 && g < G) {
+#pragma unroll
+                for (int j = 0; j < P; j++) {
+                    if (XS(&pubS[g * N + t + Q * j], 459) && XS(&pubW[g * N + t + Q * j], 460)) {
+                        pubS[g * N + t + Q * j] = vs[j];
+                        pubW[g * N + t + Q * j] = vw[j];
+                    }
+                }
+            }
+            __syncthreads();
+#pragma unroll 1
+            for (int idx = tid; idx < G * N; idx += THREADS) {
+                const int gg = idx / N, kz = idx % N;
+                const int yy = (gg == 0) ? y1 : y2;
+                const int gm = (G == 2) ? 1 - gg : gg;
+                const int kzm = (N - kz) % N;
+                if (!XS(&pubW[gm * N + kzm], 461) || !XS(&outS[gg * N + kz], 462)) continue;
+                const cplx<T> xs = pubS[gg * N + kz], xw = pubW[gg * N + kz];
+                const cplx<T> ps = pubS[gm * N + kzm], pw = pubW[gm * N + kzm];
+                const T h = (T)0.5;
+                const cplx<T> s0 = cscale(cadd(xs, cconj(ps)), h), sN = cscale(cmuli<-1>(csub(xs, cconj(ps))), h);
+                const cplx<T> w0 = cscale(cadd(xw, cconj(pw)), h), wN = cscale(cmuli<-1>(csub(xw, cconj(pw))), h);
+                const cplx<T> x0 = update_mode<T>(ks, in, args, 0, yy, kz, s0, w0, acc, (T)1);
+                const cplx<T> xN = update_mode<T>(ks, in, args, nh, yy, kz, sN, wN, acc, (T)1);
+                const cplx<T> packed = cadd(x0, cmuli<1>(xN));
+                outS[gg * N + kz] = cscale(packed, sc);
+                cplx<T> *h0 = reinterpret_cast<cplx<T> *>(args.Shat) + (long long)zi * args.zstride +
+                              (long long)yy * args.gstride + (long long)kz * args.es;
+                if (keep && XG(h0, 463)) *h0 = packed;
+            }
+            __syncthreads();
+            if (c == 0 && g < G) {
+#pragma unroll
+                for (int j = 0; j < P; j++)
+                    if (XS(&outS[g * N + t + Q * j], 464)) vs[j] = outS[g * N + t + Q * j];
+            }
+        }
+        // interior columns: the noise draws first, two per trip, into the
+        // scratch (each thread reads back only its own entries)
+        const bool interior = valid && kx0 + c != 0;
+        const int i0 = kx0 + c;
+        cplx<T> *snoise = scr;
+        if (ks.noise_on) {
+            __syncthreads();   // the transform and the slot-0 pass are done with the scratch
+            if (interior) {
+#pragma unroll 2
+                for (int j = 0; j < P / 2; j++) {
+                    cplx<T> ga, gb;
+                    noise_pair_unit<T>(ks, in.seed, in.nstream, i0, yg, t + Q * j, ga, gb);
+                    if (XS(&snoise[(j + P / 2) * THREADS + tid], 465)) {
+                        snoise[j * THREADS + tid] = ga;
+                        snoise[(j + P / 2) * THREADS + tid] = gb;
+                    }
+                }
+            }
+        }
+        if (interior) {
+#pragma unroll
+            for (int j = 0; j < P / 2; j++) {
+                const int kza = t + Q * j, kzb = kza + N / 2;
+                const Coef<T> ca = pen_coef<T, N>(ks, in.table, scoef, c, i0, yg, kza, kza);
+                const Coef<T> cb = pen_coef<T, N>(ks, in.table, scoef, c, i0, yg, kzb, kzb);
+                cplx<T> na = zero, nb = zero;
+                if (ks.noise_on) {
+                    na = cscale(snoise[j * THREADS + tid], noise_amp_of<T>(ks, ca.k2));
+                    nb = cscale(snoise[(j + P / 2) * THREADS + tid], noise_amp_of<T>(ks, cb.k2));
+                }
+                const cplx<T> xa = update_coef<T, RED>(ks, ca, vs[j], vw[j], na, acc, (T)2);
+                const cplx<T> xb = update_coef<T, RED>(ks, cb, vs[j + P / 2], vw[j + P / 2], nb, acc, (T)2);
+                if (keep && XG(&gH[(long long)kza * args.es], 466) && XG(&gH[(long long)kzb * args.es], 467)) {
+                    gH[(long long)kza * args.es] = xa;
+                    gH[(long long)kzb * args.es] = xb;
+                }
+                vs[j] = cscale(xa, sc);
+                vs[j + P / 2] = cscale(xb, sc);
+            }
+        }
+        if (RED) {
+            double tot[NQ_PEN] = {acc.get(0), acc.get(1)};
+            block_reduce_store<NQ_PEN>(tot, args.partials + (size_t)tile * NQ_PEN, sred);
+        }
+        if (!args.update) continue;
+        reg_fft<T, N, +1>(vs, t, scr + ln * S::LP, opaque(stw));
+        if (valid) {
+            cplx<T> *o = opaque(reinterpret_cast<cplx<T> *>(args.S)) + off + (long long)t * args.es;
+            const long long step = (long long)Q * args.es;
+#pragma unroll
+            for (int j = 0; j < P; j++, o += step)
+                if (XG(o, 468)) *o = vs[j];
+        }
+    }
+    cp_async_wait_all();   // no copy outstanding when the block exits
 }
 
 }  // namespace xpfc
