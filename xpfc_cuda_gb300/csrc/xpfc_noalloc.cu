@@ -29,7 +29,6 @@
 // array) is not supported.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/xpfc.h"
@@ -42,10 +41,6 @@ constexpr int kMaxChunks = XPFC_NOALLOC_MAX_CHUNKS;
 constexpr int kThreads = 256;
 
 static __device__ __align__(256) double g_fe_scratch[kMaxChunks + 1];
-
-// per device: the device address of g_fe_scratch (looked up on first use)
-std::mutex g_lock;
-double *g_addr[256] = {nullptr};
 
 // one block per chunk: sum of the FE_calc.cu:64 density over the chunk
 __global__ void __launch_bounds__(kThreads)
@@ -100,19 +95,12 @@ extern "C" int xpfc_FE_calc_noalloc(const double *psi, const double *psi2, const
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(XPFC_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= 256) return fail(XPFC_EINVAL, "device ordinal out of range");
-    double *slots = nullptr;
-    {
-        std::lock_guard<std::mutex> g(g_lock);
-        if (!g_addr[dev]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_fe_scratch);
-            if (e != cudaSuccess)
-                return fail(XPFC_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_addr[dev] = static_cast<double *>(p);
-        }
-        slots = g_addr[dev];
-    }
+    // looked up on every call (it allocates nothing): a cached address would
+    // go stale if the caller reset the device and the module was reloaded
+    void *sym = nullptr;
+    e = cudaGetSymbolAddress(&sym, g_fe_scratch);
+    if (e != cudaSuccess) return fail(XPFC_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    double *slots = static_cast<double *>(sym);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int nchunks = (int)((n + kChunk - 1) / kChunk);
     e = cudaMemsetAsync(slots + kMaxChunks, 0, sizeof(double), s);
