@@ -4,6 +4,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -257,25 +258,58 @@ static void par_chunks(size_t n, F fn) {
 }
 
 // Copies a caller's field and pins its mean to psi0 (Avg_calc.cu:21-43: the
-// difference is added to every value when the mean is not psi0).
-static void stage_and_pin(double *dst, const double *src, size_t n, double psi0) {
+// difference is added to every value when the mean is not psi0).  The 16
+// chunks run on their own threads, or one after another when the caller
+// stages several fields in parallel (the same sums either way).
+static void stage_and_pin(double *dst, const double *src, size_t n, double psi0, bool threaded = true) {
     double part[16] = {0.0};
-    par_chunks(n, [&](int k, size_t b, size_t e) {
+    auto sum_chunk = [&](int k, size_t b, size_t e) {
         double s = 0.0;
         for (size_t i = b; i < e; i++) {
             dst[i] = src[i];
             s += src[i];
         }
         part[k] = s;
-    });
+    };
+    if (threaded) {
+        par_chunks(n, sum_chunk);
+    } else {
+        for (int k = 0; k < 16; k++) sum_chunk(k, n * k / 16, n * (k + 1) / 16);
+    }
     double s = 0.0;
     for (int k = 0; k < 16; k++) s += part[k];
     const double m = s / (double)n;
     const double diff = (m != psi0) ? psi0 - m : 0.0;
-    if (diff != 0.0)
-        par_chunks(n, [&](int, size_t b, size_t e) {
-            for (size_t i = b; i < e; i++) dst[i] += diff;
-        });
+    if (diff == 0.0) return;
+    auto add_chunk = [&](int, size_t b, size_t e) {
+        for (size_t i = b; i < e; i++) dst[i] += diff;
+    };
+    if (threaded) {
+        par_chunks(n, add_chunk);
+    } else {
+        for (int k = 0; k < 16; k++) add_chunk(k, n * k / 16, n * (k + 1) / 16);
+    }
+}
+
+// Pinned host staging for the synchronous initial-field uploads
+// (xpfc_initialize, xpfc_batch_initialize), shared by every context of the
+// process and kept between calls, so that a solve started after another one
+// does not pin fresh host memory (hundreds of MB for a batch) first.  Held
+// under upload_mu from staging until the upload has completed.
+static std::mutex upload_mu;
+static void *upload_buf = nullptr;
+static size_t upload_bytes = 0;
+static void *upload_pool(size_t bytes) {
+    if (bytes <= upload_bytes) return upload_buf;
+    if (upload_buf) cudaFreeHost(upload_buf);
+    upload_buf = nullptr;
+    upload_bytes = 0;
+    if (cudaHostAlloc(&upload_buf, bytes, cudaHostAllocPortable) != cudaSuccess) {
+        upload_buf = nullptr;
+        return nullptr;
+    }
+    upload_bytes = bytes;
+    return upload_buf;
 }
 
 // Diagnostics switch XPFC_POISON=1: every state buffer is filled with
@@ -959,9 +993,9 @@ extern "C" int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi) {
         rc = enqueue_initial_field(ctx->p, dpsi, ctx->partials, ctx->stream, &why);
         if (rc != XPFC_OK) return fail(ctx, rc, why);
     } else {
-        rc = host_stage(ctx, sizeof(double) * n);
-        if (rc != XPFC_OK) return rc;
-        double *h = (double *)ctx->hstage;
+        std::lock_guard<std::mutex> g(upload_mu);
+        double *h = (double *)upload_pool(sizeof(double) * n);
+        if (!h) return fail(ctx, XPFC_ENOMEM, "pinned upload staging");
         if (host_psi) {
             stage_and_pin(h, host_psi, n, ctx->p.psi0);   // configure_avg_density, Avg_calc.cu:21-43
         } else {
@@ -969,6 +1003,7 @@ extern "C" int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi) {
             if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
         }
         XPFC_CUDA(ctx, cudaMemcpyAsync(dpsi, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // the staging is free again
     }
     rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
     if (rc != XPFC_OK) return rc;
@@ -2083,21 +2118,42 @@ static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) 
     int rc = XPFC_OK;
     bool need_host = false;
     for (size_t k = 0; k < nb; k++) need_host |= fields[k] != nullptr || !ic_on_device(ctx->inst[k]);
-    if (need_host) rc = host_stage(ctx, sizeof(double) * n * nb);
-    if (rc != XPFC_OK) return rc;
-    double *h = (double *)ctx->hstage;
+    std::unique_lock<std::mutex> up(upload_mu, std::defer_lock);
+    double *h = nullptr;
+    if (need_host) {
+        up.lock();
+        h = (double *)upload_pool(sizeof(double) * n * nb);
+        if (!h) return fail(ctx, XPFC_ENOMEM, "pinned upload staging");
+    }
     // host fields (given, or the VTK restart) go up in one copy per run of
-    // consecutive instances; the other generators run on the device
+    // consecutive instances; the other generators run on the device.  Given
+    // fields are staged on up to 16 threads, one field per thread.
     std::vector<char> on_dev(nb, 0);
+    std::vector<size_t> given;
     for (size_t k = 0; k < nb; k++) {
         if (fields[k]) {
-            stage_and_pin(h + k * n, fields[k], n, ctx->inst[k].psi0);
+            given.push_back(k);
         } else if (ic_on_device(ctx->inst[k])) {
             on_dev[k] = 1;
         } else {
             rc = build_initial_field(&ctx->inst[k], h + k * n);
             if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
         }
+    }
+    if (given.size() == 1) {
+        stage_and_pin(h + given[0] * n, fields[given[0]], n, ctx->inst[given[0]].psi0);
+    } else if (!given.empty()) {
+        std::atomic<size_t> next{0};
+        auto work = [&] {
+            for (size_t i; (i = next.fetch_add(1)) < given.size();) {
+                const size_t k = given[i];
+                stage_and_pin(h + k * n, fields[k], n, ctx->inst[k].psi0, false);
+            }
+        };
+        std::vector<std::thread> th;
+        const size_t nt = std::min<size_t>(16, given.size());
+        for (size_t w = 0; w < nt; w++) th.emplace_back(work);
+        for (auto &t : th) t.join();
     }
     double *dpsi = nullptr;
     XPFC_CUDA(ctx, cudaMallocAsync((void **)&dpsi, sizeof(double) * n * nb, ctx->stream));
@@ -2118,6 +2174,13 @@ static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) 
         k = k1;
     }
     if (e != cudaSuccess) rc = fail(ctx, XPFC_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    if (need_host) {
+        // the uploads from the shared staging are complete before it is released
+        const cudaError_t se = cudaStreamSynchronize(ctx->stream);
+        up.unlock();
+        if (se != cudaSuccess && rc == XPFC_OK)
+            rc = fail(ctx, XPFC_ECUDA, std::string("upload: ") + cudaGetErrorString(se));
+    }
     if (rc == XPFC_OK) rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
     cudaFreeAsync(dpsi, ctx->stream);
     if (rc != XPFC_OK) return rc;
