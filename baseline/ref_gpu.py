@@ -10,8 +10,12 @@ stage(ref)   copies the reference's sources from its tree (the build
              the output precision raised and nothing else changed: the free
              energy and residual printf formats (sum_reduction.cu:64,77, %0.10f
              and %0.5e -> %.17e) and the VTK writer's stream precision
-             (write_vtk.cu:8, 6 -> 17 significant digits).  baseline/_ref is
-             git-ignored: no reference source enters the repository.
+             (write_vtk.cu:8, 6 -> 17 significant digits), and into
+             baseline/_ref/src_xp: src_hp with one more edit, the powers of
+             apply_power taken in double precision (power_functions.cu:47,
+             powf -> pow), for the comparison with the library's exact-power
+             path.  baseline/_ref is git-ignored: no reference source enters
+             the repository.
 build()      on a machine with nvcc (the GPU machine; it is aarch64 there),
              compiles those sources for sm_103a as Makefile_Example:12-37 does
              (same file list, -O3; host flags without -march=native) and links:
@@ -19,7 +23,9 @@ build()      on a machine with nvcc (the GPU machine; it is aarch64 there),
                xpfc_ref        the same with baseline/xt_one_gpu.cu, which
                                serves cuFFT's multi-GPU descriptor calls on
                                one GPU (cufftXtSetGPUs refuses a single GPU);
-               xpfc_ref_hp     src_hp with xt_one_gpu.cu (full-precision output).
+               xpfc_ref_hp     src_hp with xt_one_gpu.cu (full-precision output);
+               xpfc_ref_xp     src_xp with xt_one_gpu.cu (full-precision output,
+                               double-precision powers).
              NCCL: the system's (or the CUDA Python wheel's) header and
              library when present, else the one-rank stand-in in
              baseline/nccl_one_rank (a sum reduce to root 0 over one rank is a
@@ -53,6 +59,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 SRC_HP = os.path.join(OUT, "src_hp")
+SRC_XP = os.path.join(OUT, "src_xp")
 BIN = os.path.join(OUT, "gpu")
 # Makefile_Example:29 (randn.cu is not in it and does not compile)
 UNITS = ["main", "initialize", "FFT_freq", "Avg_calc", "linspace", "read_input", "write_vtk", "convolve_fields",
@@ -70,6 +77,14 @@ HP_EDITS = [
     ("write_vtk.cu", "    ofstream vtkFile(vtkFilename);\n",
      "    ofstream vtkFile(vtkFilename);\n    vtkFile.precision(17);\n"),
 ]
+# src_xp: src_hp's edits plus the powers in double precision (the reference
+# rounds psi to float and takes powf, which makes its trajectory jump by a
+# float ulp wherever a double-rounding difference moves psi across a float
+# rounding boundary)
+XP_EDITS = HP_EDITS + [
+    ("power_functions.cu", "double a = powf(psi[i + j*Mx].x, pow_i);",
+     "double a = pow(psi[i + j*Mx].x, pow_i);"),
+]
 
 
 def _sha(path):
@@ -81,28 +96,29 @@ def stage(ref):
     """Copies the reference's sources (and the output-precision variant)."""
     if not ref or not os.path.isfile(os.path.join(ref, "main.cu")):
         raise SystemExit("stage: no reference tree at %r (give --ref or XPFC_REFERENCE)" % (ref,))
-    for d in (SRC, SRC_HP):
+    for d in (SRC, SRC_HP, SRC_XP):
         os.makedirs(d, exist_ok=True)
-    manifest = {"reference": os.path.abspath(ref), "files": {}, "hp_edits": []}
+    manifest = {"reference": os.path.abspath(ref), "files": {}, "hp_edits": [], "xp_edits": []}
     for name in [u + ".cu" for u in UNITS] + HEADERS:
-        for d in (SRC, SRC_HP):
+        for d in (SRC, SRC_HP, SRC_XP):
             shutil.copyfile(os.path.join(ref, name), os.path.join(d, name))
         manifest["files"][name] = _sha(os.path.join(SRC, name))
-    for name, old, new in HP_EDITS:
-        path = os.path.join(SRC_HP, name)
-        text = open(path).read()
-        if text.count(old) != 1:
-            raise SystemExit("stage: the output-precision edit of %s does not apply" % name)
-        with open(path, "w") as f:
-            f.write(text.replace(old, new))
-        manifest["hp_edits"].append({"file": name, "from": old, "to": new})
+    for tree, edits, key in ((SRC_HP, HP_EDITS, "hp_edits"), (SRC_XP, XP_EDITS, "xp_edits")):
+        for name, old, new in edits:
+            path = os.path.join(tree, name)
+            text = open(path).read()
+            if text.count(old) != 1:
+                raise SystemExit("stage: the edit of %s for %s does not apply" % (name, os.path.basename(tree)))
+            with open(path, "w") as f:
+                f.write(text.replace(old, new))
+            manifest[key].append({"file": name, "from": old, "to": new})
     with open(os.path.join(OUT, "MANIFEST.json"), "w") as f:
         json.dump(manifest, f, indent=1)
     return OUT
 
 
 def staged():
-    return all(os.path.isfile(os.path.join(d, "main.cu")) for d in (SRC, SRC_HP))
+    return all(os.path.isfile(os.path.join(d, "main.cu")) for d in (SRC, SRC_HP, SRC_XP))
 
 
 def _nvcc():
@@ -129,7 +145,7 @@ def _find_nccl():
 
 
 def programs():
-    return {k: os.path.join(BIN, k) for k in ("xpfc_ref_stock", "xpfc_ref", "xpfc_ref_hp")}
+    return {k: os.path.join(BIN, k) for k in ("xpfc_ref_stock", "xpfc_ref", "xpfc_ref_hp", "xpfc_ref_xp")}
 
 
 def build(force=False, log=print):
@@ -155,7 +171,7 @@ def build(force=False, log=print):
     flags = ["-O3", "-std=c++17", "-w"] + ARCH + ["-Xcompiler", "-fopenmp"] + inc
 
     jobs = []
-    for tag, src in (("src", SRC), ("src_hp", SRC_HP)):
+    for tag, src in (("src", SRC), ("src_hp", SRC_HP), ("src_xp", SRC_XP)):
         d = os.path.join(BIN, tag)
         os.makedirs(d, exist_ok=True)
         for u in UNITS:
@@ -173,12 +189,12 @@ def build(force=False, log=print):
 
     with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         list(ex.map(compile_one, jobs))
-    objs = {tag: [os.path.join(BIN, tag, u + ".o") for u in UNITS] for tag in ("src", "src_hp")}
+    objs = {tag: [os.path.join(BIN, tag, u + ".o") for u in UNITS] for tag in ("src", "src_hp", "src_xp")}
     shim = [os.path.join(BIN, "xt_one_gpu.o")]
     nccl_obj = [os.path.join(BIN, "nccl_one_rank.o")] if not nccl else []
     libs = ["-lcufft", "-lcudart", "-ldl", "-Xcompiler", "-fopenmp"] + link_nccl
     for name, ob in (("xpfc_ref_stock", objs["src"]), ("xpfc_ref", objs["src"] + shim),
-                     ("xpfc_ref_hp", objs["src_hp"] + shim)):
+                     ("xpfc_ref_hp", objs["src_hp"] + shim), ("xpfc_ref_xp", objs["src_xp"] + shim)):
         cmd = [_nvcc()] + ARCH + ob + nccl_obj + ["-o", progs[name] + ".tmp"] + libs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -8,12 +8,16 @@ make_golden.py plus two 512^2 decks (the 64^3-point 2-D analogue: dx = 0.125,
 a seeded noise liquid read through the iconfig = 10 restart, 61 and 2001
 loop iterations).  Each deck gives tests/golden/gpu_<name>.npz with the
 full-precision F and residual series and final field, the same series from the
-unmodified-output build, and the run's metadata.  Also probes the build linked
+unmodified-output build, and the run's metadata.  With --exact-powers it runs
+the 512^2 decks on the build whose apply_power takes its powers in double
+precision (power_functions.cu:47, powf -> pow; nothing else changed) and
+writes tests/golden/gpu_xp_<name>.npz.  Also probes the build linked
 against cuFFT as shipped (whose cufftXtSetGPUs is given one GPU) and times the
 reference loop (its TIMING line, main.cu:305,437) at 512^2 and 4096^2.
 
 Usage (GPU machine, sources staged):
     python tests/golden/make_golden_gpu.py [--out DIR] [--no-timing]
+    python tests/golden/make_golden_gpu.py --exact-powers [--out DIR]
 """
 import argparse
 import json
@@ -81,15 +85,53 @@ def meta():
     return m
 
 
+def _vtk_extra(name, vtk_in):
+    # small restart fields are stored; the 512^2 one is regenerated from its seed
+    if vtk_in is None:
+        return {}
+    if vtk_in.size <= 4096:
+        return {"vtk_in": vtk_in}
+    return {"vtk_seed": np.array([NOISE512_SEED]),
+            "vtk_amp": np.array([0.05 if name.startswith("noise512q") else 0.1])}
+
+
+def exact_powers(progs, info, out):
+    """The 512^2 decks on the double-precision-power build (gpu_xp_*.npz)."""
+    info = dict(info, variant="power_functions.cu:47 powf -> pow (double-precision powers), 17-digit output")
+    for name, text, vtk_in in gpu_cases():
+        if not name.startswith("noise512"):
+            continue
+        ts = t_sample_of(text)
+        vtk = vtk_text(vtk_in, dims_of(vtk_in), dims_of(vtk_in), 0.125)
+        xp = ref_gpu.run(progs["xpfc_ref_xp"], text, ts, vtk_in=vtk, timeout=900)
+        if xp["returncode"] != 0 or "psi_final" not in xp:
+            print(name, "FAILED", xp["returncode"], xp["stdout_tail"][-1500:], xp["stderr_tail"][-1500:], flush=True)
+            continue
+        np.savez_compressed(
+            os.path.join(out, "gpu_xp_%s.npz" % name),
+            deck=np.frombuffer(text.encode(), dtype=np.uint8),
+            F=np.array(xp["F"], dtype=np.float64).reshape(-1, 2),
+            RMS=np.array(xp["RMS"], dtype=np.float64).reshape(-1, 2),
+            psi_final=xp["psi_final"],
+            final_iteration=np.array([xp["final_iteration"]]),
+            meta=np.frombuffer(json.dumps(dict(info, timing=xp["timing"])).encode(), dtype=np.uint8),
+            **_vtk_extra(name, vtk_in))
+        print("xp", name, "F", xp["F"][:2], "...", xp["F"][-1:], "timing", xp["timing"], flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--no-timing", action="store_true")
     ap.add_argument("--only", default=None, help="comma-separated deck names")
+    ap.add_argument("--exact-powers", action="store_true")
     a = ap.parse_args()
     os.makedirs(a.out, exist_ok=True)
     progs = ref_gpu.build()
     info = meta()
+    if a.exact_powers:
+        exact_powers(progs, info, a.out)
+        return
 
     # the program linked against cuFFT as shipped, on the smallest deck
     name, text, vtk_in = gpu_cases()[2]
@@ -109,14 +151,7 @@ def main():
             print(name, "FAILED", hp["returncode"], lo["returncode"], hp["stdout_tail"][-1500:],
                   hp["stderr_tail"][-1500:], flush=True)
             continue
-        # small restart fields are stored; the 512^2 one is regenerated from its seed
-        extra = {}
-        if vtk_in is not None:
-            if vtk_in.size <= 4096:
-                extra = {"vtk_in": vtk_in}
-            else:
-                extra = {"vtk_seed": np.array([NOISE512_SEED]),
-                         "vtk_amp": np.array([0.05 if name.startswith("noise512q") else 0.1])}
+        extra = _vtk_extra(name, vtk_in)
         np.savez_compressed(
             os.path.join(a.out, "gpu_%s.npz" % name),
             deck=np.frombuffer(text.encode(), dtype=np.uint8),

@@ -74,19 +74,22 @@ def test_reference_fixtures_record_the_one_gpu_build():
 # Tolerances: (field rel-L2, F rel, residual RMS rel, last iteration whose RMS
 # is compared).  Measured on GB300: the four small decks (16^2 to 64^2, 11 to
 # 81 iterations) agree with the reference's run to F 1e-13 and field 3e-15.
-# The 512^2 decks agree to F about 4e-12 after 100 iterations and drift to F
-# 5e-9 and field 1.2e-8 after 2001 (F 3e-11, field 6e-10 after 61), with
-# either noise amplitude.  The library's staged loop and its fused step agree
-# with each other far closer than either does with the reference, so the
-# difference is systematic, and the obvious sources are ruled out by
-# measurement: both FP64 transforms have the same accuracy against numpy
-# (rms 3.5e-16 ours, 3.4e-16 cuFFT at 512^2), the device powf of the
-# reference's apply_power kernel and the library's are bit-identical on 4M
-# inputs for powers 2, 3 and 4, and the two roundings of the coefficients
-# (kx^2 + ky^2 and a division, against shell tables and a multiplication)
-# change F by 2e-16 over the same 100 steps.  The residual RMS of these
-# relaxed liquids (a float-squared residual, sse_calculation.cu:38) is
-# resolved only at the first sample.
+# The 512^2 noise decks agree to F about 4e-12 after 100 iterations and drift
+# to F 5e-9 and field 1.2e-8 after 2001 (F 3e-11, field 6e-10 after 61).  The
+# cause is the reference's float power (power_functions.cu:47): apply_power
+# rounds psi to float before powf, so the map jumps by a float ulp (about
+# 4e-9 at psi = 0.05) wherever a double-rounding difference of the transforms
+# moves psi across a float rounding boundary, and once a few points have
+# jumped the difference spreads to that float-rounding level.  Any two FP64
+# transforms show it: the oracle's loop with numpy's FFT in place of its own
+# (same powers, same tables) leaves the oracle by 3e-16 after 61 iterations,
+# 4e-11 after 150 and 5e-10 after 400 at 512^2, and by 2e-16 with exact powers
+# (tests/test_oracle_sensitivity.py).  With the powers in double precision on
+# both sides (the reference built with pow in place of powf) the library
+# matches the reference's run at 512^2 over 2001 iterations to the
+# spec bar (test_exact_powers_match_reference_gpu_run).  The residual
+# RMS of these relaxed liquids (a float-squared residual,
+# sse_calculation.cu:38) is resolved only at the first sample.
 TOL = {"noise512_t60": (2e-9, 1e-10, 1e-6, 0), "noise512_t2000": (5e-8, 1e-8, 1e-6, 0),
        "noise512q_t2000": (5e-8, 1e-8, 1e-6, 0)}
 DEFAULT_TOL = (1e-10, 1e-12, 1e-8, None)
@@ -126,3 +129,39 @@ def test_fused_step_matches_reference_gpu_run(name, tmp_path):
             seen += 1
     assert seen >= 2
     assert rel_l2(field, z["psi_final"]) <= ftol
+
+
+# The reference built with its powers in double precision (apply_power's powf
+# -> pow, power_functions.cu:47, and nothing else; tests/golden/
+# make_golden_gpu.py --exact-powers) against the library in the same
+# semantics: the reference's two-peak sum kernel, ff_factor and step count,
+# exact powers (ref_compat = 0; the integer Mo of the residual is 1 in these
+# decks either way).  Without the float rounding of psi the two FP64 paths do
+# not drift apart: field rel-L2 <= 1e-10 and F rel <= 1e-12 at every printed
+# iteration, over 61 and 2001 iterations of 512^2.
+XP_CASES = ["noise512_t60", "noise512_t2000", "noise512q_t2000"]
+
+
+@pytest.mark.parametrize("name", XP_CASES)
+def test_exact_powers_match_reference_gpu_run(name, tmp_path):
+    import xpfc_cuda_gb300 as X
+    z, p, psi0 = _case(X, "xp_" + name, tmp_path)
+    p.ref_compat = 0
+    with X.Xpfc(p) as x:
+        x.initialize(psi0)
+        F, _ = X.run_reference_loop(x, p.nsteps, p.t_sample)
+        staged = x.download(X._lib.BUF_PSI_NP1_R)
+    with X.Xpfc(p) as x:
+        x.initialize(psi0)
+        recs = x.step(p.nsteps)
+        fused = x.copy2cpu().reshape(-1)
+    got = {r["iteration"]: r["F"] for r in recs if r["F"] is not None}
+    seen = 0
+    for it, v in z["F"]:
+        assert abs(F[int(it)] - v) <= 1e-12 * abs(v), ("staged", it, F[int(it)], v)
+        if int(it) in got:
+            assert abs(got[int(it)] - v) <= 1e-12 * abs(v), ("fused", it, got[int(it)], v)
+            seen += 1
+    assert seen >= 2
+    assert rel_l2(staged, z["psi_final"]) <= 1e-10
+    assert rel_l2(fused, z["psi_final"]) <= 1e-10
