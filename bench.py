@@ -19,7 +19,9 @@ restating the reference's loop, OpenMP on the host cores), rank 0 only.
 Three more legs ride on the same line: "sweep" (64 independent solves of
 1000 steps through one xpfc_batch: solves/s, against the same solves one
 context at a time), "serve" (a Poisson stream of solve requests through
-xpfc_server: latency percentiles and served grid-point-steps/s) and "two_d"
+xpfc_server: latency percentiles and served grid-point-steps/s, every solve
+in a context of its own, then with merged groups, and a stream of 64^3
+requests both ways) and "two_d"
 (the 2-D step at 4096^2, the reference's own benchmark size, both
 precisions).
 
@@ -341,27 +343,56 @@ def run_serve(args, rank, local, group, barrier):
     # a few of the smaller requests keep their fields for the same-as-alone check
     keep = [i for i, (_, p, k) in enumerate(stream) if p.Mx <= 96 and k <= 2000][:3]
     budget = 150 << 30
-    with X.Server(hbm_budget_bytes=budget, max_running=args.serve_running, chunk_steps=16, device=local) as srv:
-        # warm server: one short solve of every size (kernel modules loaded, one
-        # pooled context per size)
-        warm = [srv.submit(p, 3) for p in {p.Mx: p for _, p, _ in stream}.values()]
-        for w in warm:
-            srv.wait(w)
-        barrier()
-        ids, recs, span = SV.play(srv, stream, set(keep))
-        barrier()
-        stats = srv.stats()
-        same = True
-        for i in keep:
-            _, p, k = stream[i]
-            f, r = srv.result(ids[i], shape=(p.Mx, p.My, p.Mz))
-            with X.Xpfc(p) as x:
-                x.initialize(None)
-                r1 = x.step(k)
-                f1 = x.copy2cpu()
-            same &= bool(np.array_equal(f, f1) and r == r1)
+
+    def play(strm, merge_max, keep_ids=()):
+        with X.Server(hbm_budget_bytes=budget, max_running=args.serve_running, chunk_steps=16, device=local,
+                      merge_max=merge_max) as srv:
+            # warm server: one short solve of every size (kernel modules loaded,
+            # one pooled context per size)
+            warm = [srv.submit(p, 3) for p in {p.Mx: p for _, p, _ in strm}.values()]
+            for w in warm:
+                srv.wait(w)
+            barrier()
+            ids, recs, span = SV.play(srv, strm, set(keep_ids))
+            barrier()
+            stats = srv.stats()
+            same = True
+            for i in keep_ids:
+                _, p, k = strm[i]
+                f, r = srv.result(ids[i], shape=(p.Mx, p.My, p.Mz))
+                with X.Xpfc(p) as x:
+                    x.initialize(None)
+                    r1 = x.step(k)
+                    f1 = x.copy2cpu()
+                same &= bool(np.array_equal(f, f1) and r == r1)
+        return recs, span, stats, same
+
+    def brief(recs, span, stats, same, r):
+        o = SV.summarise(recs, span, r)
+        return {"solves_per_s": len(recs) / span, "latency_p50_s": o["latency_p50_s"],
+                "latency_p99_s": o["latency_p99_s"], "served_gpt_steps_per_s": o["served_gpt_steps_per_s"],
+                "merged_groups": stats["merged_groups"], "merged_solves": stats["merged_solves"],
+                "same_as_alone": same}
+
+    recs, span, stats, same = play(stream, 0, keep)
     out = SV.summarise(recs, span, rate)
     out["solves_per_s"] = len(recs) / span
+    if args.serve_merge > 1:
+        # the same stream with merged groups (queued requests of one grid with
+        # step counts within 25 % share every launch)
+        m = brief(*play(stream, args.serve_merge, keep), rate)
+        m["merge_max"] = args.serve_merge
+        out["with_merging"] = m
+        same &= m["same_as_alone"]
+        # a stream of 64^3 requests alone (passes bound by launch latency),
+        # without and with merging
+        srate = 100.0
+        small = SV.request_stream(200, rate=srate, seed=100 + rank, sizes=(64,), weights=(1.0,), device=local)
+        s0 = brief(*play(small, 0), srate)
+        s1 = brief(*play(small, args.serve_merge), srate)
+        out["small_grid_stream"] = {"workload": "200 requests of 64^3, Poisson 100/s, steps U[200,5000], "
+                                                "sweep physics", "without_merging": s0, "with_merging": s1,
+                                    "solves_per_s_ratio": s1["solves_per_s"] / s0["solves_per_s"]}
     if not args.no_serve_seq:
         # the plain sequential baselines: the same requests one at a time, each
         # alone, in FP64 and in mixed precision (estimated per grid size)
@@ -556,6 +587,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serve-running", type=int, default=16)
+    ap.add_argument("--serve-merge", type=int, default=8,
+                    help="solves per merged group in the serving leg's merged runs (0: no merged runs)")
     ap.add_argument("--no-serve-seq", action="store_true", help="skip the sequential baselines of the serve leg")
     ap.add_argument("--no-two-d", action="store_true")
     ap.add_argument("--two-d-size", type=int, default=4096)

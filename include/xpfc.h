@@ -260,19 +260,28 @@ int xpfc_batch_get_field(xpfc_batch *b, int i, double *host_psi);
 /* No counterpart in the reference, which runs one solve per process.  A server
    runs solve requests on one GPU from a scheduler thread of its own: queued
    requests are admitted in arrival order while their device memory fits
-   hbm_budget_bytes and fewer than max_running solves are in flight; each
+   hbm_budget_bytes and fewer than max_running contexts are in flight; each
    running solve has a context with its own stream (reused across requests of
    the same grid and precision) and its iterations are enqueued chunk_steps at
    a time, round robin, so solves join and leave the running set at chunk
-   boundaries while the GPU interleaves them.  A request's diagnostics and
-   field are those xpfc_step gives for the same params alone.  Initial fields
-   come from the params' generator on the device, or from the caller. */
+   boundaries while the GPU interleaves them.  With merge_max > 1, queued
+   requests of the same grid that agree on everything but psi0, sigma, the
+   peaks, the seeds and the initial field (the xpfc_batch grouping rule,
+   equal box lengths), and whose step counts lie within 25 % of each other,
+   are admitted together, up to merge_max at a time, as one merged group: a
+   batched context whose every pass covers all of them in one launch (grid z =
+   solve), counted once against max_running.  The group runs to its longest solve; a shorter solve's field is
+   read back at its own last iteration and its results are handed over when
+   the group finishes.  A request's diagnostics and field are those xpfc_step
+   gives for the same params alone, merged or not.  Initial fields come from
+   the params' generator on the device, or from the caller. */
 typedef struct xpfc_server xpfc_server;
 typedef struct {
     size_t hbm_budget_bytes;  /* device memory for solves (0: 80% of free memory) */
-    int max_running;          /* solves in flight (0: 16)                        */
+    int max_running;          /* contexts in flight, a merged group once (0: 16) */
     int chunk_steps;          /* iterations per solve per round (0: 16)          */
     int device;
+    int merge_max;            /* solves per merged group (0 or 1: no merging)    */
 } xpfc_server_config;
 typedef enum { XPFC_REQ_QUEUED = 0, XPFC_REQ_RUNNING = 1, XPFC_REQ_DONE = 2, XPFC_REQ_FAILED = 3 } xpfc_req_state;
 typedef struct {
@@ -286,6 +295,7 @@ typedef struct {
     long long submitted, queued, running, done, failed;
     long long contexts_created, contexts_reused;
     size_t bytes_in_use, peak_bytes_in_use, budget;
+    long long merged_groups, merged_solves;   /* groups formed, solves they held */
 } xpfc_server_stats;
 int xpfc_server_create(const xpfc_server_config *cfg, xpfc_server **out);
 /* Running solves finish; queued ones fail (XPFC_ESTATE). */

@@ -110,3 +110,121 @@ def test_server_stop_fails_queued_requests():
     ids = [s.submit(p, 200) for _ in range(4)]
     s.wait(ids[0], timeout=120.0)
     s.close()
+
+
+def _solve_bytes(N, esz, two_d=False):
+    """Device bytes the server books for one solve (S, W, read-back, the FP64
+    initial field while it is prepared, tables): grids without a kept
+    spectrum."""
+    cells = N ** 2 if two_d else N ** 3
+    return 3 * esz * cells + 8 * cells + (4 << 20)
+
+
+def _serve_behind_blocker(X, reqs, merge_max, extra_budget=0):
+    """Runs reqs [(params, steps, field)] on a server whose budget holds a
+    128^3 FP64 blocker alone: the blocker is admitted first and the requests
+    queue behind it, so that the groups they can form are formed when it
+    finishes.  Returns ([(field, records)], stats)."""
+    D = X._lib.FP64
+    blocker = _params(X, 128, D, 0.05, 0.25, SINGLE_PEAK, 0.0, 99)
+    smallest = min(_solve_bytes(p.Mx, 4 if p.precision == X._lib.MIXED else 8, p.Mz == 1) for p, _, _ in reqs)
+    budget = _solve_bytes(128, 8) + smallest - 1 + extra_budget
+    with X.Server(hbm_budget_bytes=budget, max_running=16, chunk_steps=5, merge_max=merge_max) as s:
+        b = s.submit(blocker, 300)
+        ids = [s.submit(p, n, field=f, keep_field=True) for p, n, f in reqs]
+        s.wait(b, timeout=120.0)
+        out = []
+        for rid, (p, n, f) in zip(ids, reqs):
+            s.wait(rid, timeout=120.0)
+            try:
+                out.append(s.result(rid, shape=(p.Mx, p.My, p.Mz)))
+            except X.XpfcError as e:
+                out.append(e)
+        st = s.stats()
+    assert st["peak_bytes_in_use"] <= budget
+    return out, st
+
+
+def test_server_merged_groups_equal_single_runs():
+    """Queued requests of one grid with step counts within 25 % run as merged
+    groups (one launch per pass for all of them); each result is bit for bit
+    the solve alone, including solves that end before their group's last
+    iteration (final free energy and field taken there) and a caller's field."""
+    import xpfc_cuda_gb300 as X
+    M, D = X._lib.MIXED, X._lib.FP64
+    given = X.build_initial_field(_params(X, 64, M, 0.05, 0.25, SINGLE_PEAK, 0.01, 13))
+    reqs = [
+        (_params(X, 64, M, 0.04, 0.22, FCC_PEAKS, 0.01, 11), 40, None),
+        (_params(X, 64, M, 0.06, 0.28, SINGLE_PEAK, 0.01, 12), 37, None),
+        (_params(X, 64, M, 0.05, 0.25, SINGLE_PEAK, 0.01, 13), 34, given),
+        (_params(X, 64, M, 0.03, 0.3, FCC_PEAKS, 0.01, 14), 42, None),
+        (_params(X, 128, M, 0.04, 0.22, FCC_PEAKS, 0.01, 15, two_d=True), 30, None),
+        (_params(X, 128, M, 0.05, 0.25, SINGLE_PEAK, 0.01, 16, two_d=True), 28, None),
+        (_params(X, 128, M, 0.02, 0.3, FCC_PEAKS, 0.01, 17, two_d=True), 25, None),
+        (_params(X, 32, D, 0.03, 0.25, SINGLE_PEAK, 0.0, 18), 20, None),
+        (_params(X, 32, D, 0.05, 0.22, FCC_PEAKS, 0.0, 19), 24, None),
+        # step count outside the 64^3 group's band: runs alone
+        (_params(X, 64, M, 0.04, 0.25, SINGLE_PEAK, 0.01, 20), 100, None),
+    ]
+    got, st = _serve_behind_blocker(X, reqs, merge_max=4)
+    assert st["merged_groups"] == 3 and st["merged_solves"] == 9, st
+    assert st["done"] == len(reqs) + 1 and st["failed"] == 0, st
+    for k, ((p, n, f), res) in enumerate(zip(reqs, got)):
+        assert not isinstance(res, Exception), (k, res)
+        field, recs = res
+        f1, r1 = _alone(X, p, n, f)
+        assert np.array_equal(field, f1), (k, float(np.nanmax(np.abs(field - f1))))
+        assert recs == r1, k
+        assert recs[-1]["iteration"] == n and recs[-1]["F"] is not None and recs[-1]["rms"] is None, k
+
+
+def test_server_merged_group_keeps_failures_local():
+    """A non-finite solve in a merged group fails alone (ENONFINITE); its
+    group's other solves are the solves alone."""
+    import xpfc_cuda_gb300 as X
+    M = X._lib.MIXED
+    reqs = [
+        (_params(X, 32, M, 0.04, 0.22, FCC_PEAKS, 0.01, 21), 30, None),
+        (_params(X, 32, M, 0.05, 0.25, SINGLE_PEAK, 0.01, 22), 27, np.full(32 ** 3, np.nan)),
+        (_params(X, 32, M, 0.03, 0.3, FCC_PEAKS, 0.01, 23), 33, None),
+    ]
+    got, st = _serve_behind_blocker(X, reqs, merge_max=8)
+    assert st["merged_groups"] == 1 and st["merged_solves"] == 3, st
+    assert isinstance(got[1], X.XpfcError) and "ENONFINITE" in str(got[1])
+    for k in (0, 2):
+        p, n, f = reqs[k]
+        f1, r1 = _alone(X, p, n, f)
+        assert np.array_equal(got[k][0], f1), k
+        assert got[k][1] == r1, k
+
+
+def test_server_merged_group_context_reused():
+    """A finished merged group's context goes to the pool; the next group of
+    the same grid and size takes it with new params (tables, pinned means,
+    seeds) and still gives every solve's results alone."""
+    import xpfc_cuda_gb300 as X
+    M, D = X._lib.MIXED, X._lib.FP64
+    blocker = _params(X, 128, D, 0.05, 0.25, SINGLE_PEAK, 0.0, 99)
+    waves = [[(_params(X, 32, M, 0.04, 0.22, FCC_PEAKS, 0.01, 31), 30),
+              (_params(X, 32, M, 0.05, 0.25, SINGLE_PEAK, 0.01, 32), 27)],
+             [(_params(X, 32, M, 0.02, 0.3, SINGLE_PEAK, 0.01, 33), 26),
+              (_params(X, 32, M, 0.06, 0.28, FCC_PEAKS, 0.01, 34), 31)]]
+    # one context in flight (a merged group counts once): each wave queues
+    # behind its blocker and forms its group when the blocker finishes
+    with X.Server(max_running=1, chunk_steps=5, merge_max=8) as s:
+        got = []
+        for wave in waves:
+            b = s.submit(blocker, 200)
+            ids = [s.submit(p, n, keep_field=True) for p, n in wave]
+            s.wait(b, timeout=120.0)
+            for rid, (p, n) in zip(ids, wave):
+                s.wait(rid, timeout=120.0)
+                got.append(s.result(rid, shape=(p.Mx, p.My, p.Mz)))
+        st = s.stats()
+    assert st["merged_groups"] == 2 and st["merged_solves"] == 4, st
+    # the blocker's context and the first group's are reused by the second wave
+    assert st["contexts_created"] == 2 and st["contexts_reused"] == 2, st
+    for (p, n), (f, recs) in zip(waves[0] + waves[1], got):
+        f1, r1 = _alone(X, p, n)
+        assert np.array_equal(f, f1)
+        assert recs == r1

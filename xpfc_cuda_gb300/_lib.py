@@ -58,7 +58,7 @@ REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
 
 class XpfcServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_running", C.c_int), ("chunk_steps", C.c_int),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("merge_max", C.c_int)]
 
 
 class XpfcRequestInfo(C.Structure):
@@ -70,7 +70,8 @@ class XpfcServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("queued", C.c_longlong), ("running", C.c_longlong),
                 ("done", C.c_longlong), ("failed", C.c_longlong), ("contexts_created", C.c_longlong),
                 ("contexts_reused", C.c_longlong), ("bytes_in_use", C.c_size_t),
-                ("peak_bytes_in_use", C.c_size_t), ("budget", C.c_size_t)]
+                ("peak_bytes_in_use", C.c_size_t), ("budget", C.c_size_t), ("merged_groups", C.c_longlong),
+                ("merged_solves", C.c_longlong)]
 
 
 # (name, restype, argtypes) for every entry point of include/xpfc.h

@@ -373,11 +373,14 @@ class Batch:
 
 class Server:
     """Solve requests on one GPU (an xpfc_server): admission under a device
-    memory budget, up to max_running solves interleaved on their own streams."""
+    memory budget, up to max_running solves interleaved on their own streams;
+    merge_max > 1 admits queued requests of the same grid and compatible
+    params (step counts within 25 %) together as merged groups of up to
+    merge_max solves that share every launch."""
 
-    def __init__(self, hbm_budget_bytes=0, max_running=16, chunk_steps=16, device=0):
+    def __init__(self, hbm_budget_bytes=0, max_running=16, chunk_steps=16, device=0, merge_max=0):
         self._L = _lib.load()
-        cfg = _lib.XpfcServerConfig(hbm_budget_bytes, max_running, chunk_steps, device)
+        cfg = _lib.XpfcServerConfig(hbm_budget_bytes, max_running, chunk_steps, device, merge_max)
         h = C.c_void_p()
         rc = self._L.xpfc_server_create(C.byref(cfg), C.byref(h))
         if rc != _lib.OK:

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -138,6 +139,9 @@ struct xpfc_ctx {
     std::map<long long, int> diag_slot;   // iteration -> slot
     long long diag_it0 = 0, diag_fin = 0;
     bool diag_final = false, diag_pending = false;
+    // further iterations whose free energy the schedule takes (a merged
+    // server group: the final iterations of its shorter solves)
+    std::set<long long> diag_extra;
     // per-pass profiling with CUDA events
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -1234,7 +1238,8 @@ static int launch_xy_pass(xpfc_ctx *ctx, int want_red, int *nb) {
 static bool diag_wantF(const xpfc_ctx *ctx, long long i) {
     const int ts = ctx->p.t_sample;
     if (i == ctx->diag_it0) return ctx->diag_it0 == 0;
-    return (ctx->diag_final && i == ctx->diag_fin) || (ts > 0 && i % ts == 0);
+    return (ctx->diag_final && i == ctx->diag_fin) || (ts > 0 && i % ts == 0) ||
+           (i < ctx->diag_fin && ctx->diag_extra.count(i));
 }
 static bool diag_wantR(const xpfc_ctx *ctx, long long i) {
     const int ts = ctx->p.t_sample;
@@ -1251,20 +1256,18 @@ static int enqueue_begin(xpfc_ctx *ctx, long long nsteps, bool final_F) {
     ctx->diag_fin = fin;
     ctx->diag_final = final_F;
     std::vector<long long> &its = ctx->diag_its;
-    its.clear();
     std::map<long long, int> &slot = ctx->diag_slot;
     slot.clear();
-    auto add = [&](long long i) {
-        if (!slot.count(i)) {
-            slot[i] = (int)its.size();
-            its.push_back(i);
-        }
-    };
-    if (diag_wantF(ctx, it0) || diag_wantR(ctx, it0)) add(it0);
+    std::set<long long> want;   // in increasing order
+    if (diag_wantF(ctx, it0) || diag_wantR(ctx, it0)) want.insert(it0);
     if (ts > 0)
         for (long long i = ((it0 / ts) + 1) * ts; i <= fin; i += ts)
-            if (diag_wantF(ctx, i) || diag_wantR(ctx, i)) add(i);
-    if (final_F) add(fin);
+            if (diag_wantF(ctx, i) || diag_wantR(ctx, i)) want.insert(i);
+    for (long long i : ctx->diag_extra)
+        if (i > it0 && i < fin) want.insert(i);
+    if (final_F) want.insert(fin);
+    its.assign(want.begin(), want.end());
+    for (size_t k = 0; k < its.size(); k++) slot[its[k]] = (int)k;
     // slots: [instance][diagnostics iteration][8]
     const int ns = (int)its.size();
     const int nbi = ctx->nb;
@@ -2112,7 +2115,9 @@ extern "C" int xpfc_batch_group_of(const xpfc_batch *b, int i) {
     return (b && i >= 0 && i < (int)b->where.size()) ? b->where[i].first : -1;
 }
 
-static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) {
+// sync: wait for the set-up on the context's stream before returning (the
+// server's merged groups skip it; their steps are ordered after it anyway)
+static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields, bool sync = true) {
     XPFC_CUDA(ctx, cudaSetDevice(ctx->p.device));
     const size_t n = (size_t)ctx->ncells, nb = (size_t)ctx->nb;
     int rc = XPFC_OK;
@@ -2184,7 +2189,7 @@ static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields) 
     if (rc == XPFC_OK) rc = ctx->esz == 4 ? init_fused<float>(ctx, dpsi) : init_fused<double>(ctx, dpsi);
     cudaFreeAsync(dpsi, ctx->stream);
     if (rc != XPFC_OK) return rc;
-    XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (sync) XPFC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->iteration = 0;
     ctx->initialized = true;
     ctx->diag_pending = false;
