@@ -134,10 +134,12 @@ int xpfc_get_params(const xpfc_ctx *ctx, xpfc_params *p);
 /* Host pointer to the stream the context launches on (cudaStream_t). */
 void *xpfc_get_stream(const xpfc_ctx *ctx);
 
-/* initialize.cu:6-238 + main.cu:226: builds (host_psi == NULL: on the device,
-   except the VTK restart, read on the host) or takes the initial field, pins
-   its mean to psi0 (Avg_calc.cu:21-43), uploads it and prepares both the
-   staged buffers (XPFC_BUF_PSI) and the fused state. */
+/* initialize.cu:6-238 + main.cu:226: builds (host_psi == NULL: the noise
+   liquid and fcc seed on the device, the reference's lattices, seeds and VTK
+   restart on the host) or takes the initial field, pins its mean to psi0
+   (Avg_calc.cu:21-43; for XPFC_IC_REFERENCE params with the reference's own
+   summation order, one running sum in index order), uploads it and prepares
+   both the staged buffers (XPFC_BUF_PSI) and the fused state. */
 int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi);
 /* The initial field of p on the host (every generator, mean pinned). */
 int xpfc_build_initial_field(const xpfc_params *p, double *host_psi);

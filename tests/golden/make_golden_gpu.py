@@ -9,9 +9,10 @@ a seeded noise liquid read through the iconfig = 10 restart, 61 and 2001
 loop iterations).  Each deck gives tests/golden/gpu_<name>.npz with the
 full-precision F and residual series and final field, the same series from the
 unmodified-output build, and the run's metadata.  With --exact-powers it runs
-the 512^2 decks on the build whose apply_power takes its powers in double
-precision (power_functions.cu:47, powf -> pow; nothing else changed) and
-writes tests/golden/gpu_xp_<name>.npz.  Also probes the build linked
+the 512^2 decks and a 4096^2 triangle-lattice deck on the build whose
+apply_power takes its powers in double precision (power_functions.cu:47,
+powf -> pow; nothing else changed) and writes tests/golden/gpu_xp_<name>.npz
+(the 4096^2 field as every 16th point in each direction).  Also probes the build linked
 against cuFFT as shipped (whose cufftXtSetGPUs is given one GPU) and times the
 reference loop (its TIMING line, main.cu:305,437) at 512^2 and 4096^2.
 
@@ -95,27 +96,42 @@ def _vtk_extra(name, vtk_in):
             "vtk_amp": np.array([0.05 if name.startswith("noise512q") else 0.1])}
 
 
-def exact_powers(progs, info, out):
-    """The 512^2 decks on the double-precision-power build (gpu_xp_*.npz)."""
+# the 2-D benchmark size (4096^2, as many points as 256^3): the reference's
+# triangle lattice with a Gaussian seed, 101 iterations; its final field is
+# stored as every SAMPLE-th point in each direction
+TRI4096 = ("tri4096_t25", deck(0.05, 0.25, 1, 3, 0.1, 1, 512, 512, 4096, 4096, 25, 0.25, 20, 0,
+                               iseed=1, ishape=1, h=4.0, k=4.0, roa=6.0))
+SAMPLE = 16
+
+
+def exact_powers(progs, info, out, only=None):
+    """The 512^2 decks and the 4096^2 deck on the double-precision-power build
+    (gpu_xp_*.npz)."""
     info = dict(info, variant="power_functions.cu:47 powf -> pow (double-precision powers), 17-digit output")
-    for name, text, vtk_in in gpu_cases():
-        if not name.startswith("noise512"):
+    runs = [(name, text, vtk_in) for name, text, vtk_in in gpu_cases() if name.startswith("noise512")]
+    runs.append(TRI4096 + (None,))
+    for name, text, vtk_in in runs:
+        if only and name not in only.split(","):
             continue
         ts = t_sample_of(text)
-        vtk = vtk_text(vtk_in, dims_of(vtk_in), dims_of(vtk_in), 0.125)
-        xp = ref_gpu.run(progs["xpfc_ref_xp"], text, ts, vtk_in=vtk, timeout=900)
+        vtk = vtk_text(vtk_in, dims_of(vtk_in), dims_of(vtk_in), 0.125) if vtk_in is not None else None
+        xp = ref_gpu.run(progs["xpfc_ref_xp"], text, ts, vtk_in=vtk, timeout=1800)
         if xp["returncode"] != 0 or "psi_final" not in xp:
             print(name, "FAILED", xp["returncode"], xp["stdout_tail"][-1500:], xp["stderr_tail"][-1500:], flush=True)
             continue
+        field = {"psi_final": xp["psi_final"]}
+        if xp["psi_final"].size > 512 * 512:
+            nx, ny = xp["dims"][0], xp["dims"][1]
+            field = {"psi_sample": xp["psi_final"].reshape(nx, ny)[::SAMPLE, ::SAMPLE].copy(),
+                     "sample_stride": np.array([SAMPLE])}
         np.savez_compressed(
             os.path.join(out, "gpu_xp_%s.npz" % name),
             deck=np.frombuffer(text.encode(), dtype=np.uint8),
             F=np.array(xp["F"], dtype=np.float64).reshape(-1, 2),
             RMS=np.array(xp["RMS"], dtype=np.float64).reshape(-1, 2),
-            psi_final=xp["psi_final"],
             final_iteration=np.array([xp["final_iteration"]]),
             meta=np.frombuffer(json.dumps(dict(info, timing=xp["timing"])).encode(), dtype=np.uint8),
-            **_vtk_extra(name, vtk_in))
+            **field, **_vtk_extra(name, vtk_in))
         print("xp", name, "F", xp["F"][:2], "...", xp["F"][-1:], "timing", xp["timing"], flush=True)
 
 
@@ -130,7 +146,7 @@ def main():
     progs = ref_gpu.build()
     info = meta()
     if a.exact_powers:
-        exact_powers(progs, info, a.out)
+        exact_powers(progs, info, a.out, a.only)
         return
 
     # the program linked against cuFFT as shipped, on the smallest deck

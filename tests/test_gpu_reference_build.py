@@ -52,12 +52,14 @@ def _case(X, name, tmp_path):
     if vtk is not None:
         (tmp_path / "initial_density_field.vtk").write_text(_vtk_text(vtk, int(round(math.sqrt(vtk.size)))))
     p = X.read_input(str(tmp_path / "pfc.input"))
-    assert p.ref_compat == 1 and p.Mz == 1
+    assert p.ref_compat == 1 and p.Mz == 1 and p.ic_kind == X._lib.IC_REFERENCE
     assert p.nsteps == int(z["final_iteration"][0])
     # the reference's restart stores the file's values in file order into its
     # [Mx][My] array (read_input.cu:208-218); xpfc_initialize pins the mean
-    # as configure_avg_density does (Avg_calc.cu:21-43)
-    psi0 = vtk.copy() if vtk is not None else X.build_initial_field(p)
+    # once, as configure_avg_density does (Avg_calc.cu:21-43).  The other
+    # decks' fields are built by xpfc_initialize itself (psi0 None), pinned
+    # once as the reference pins them.
+    psi0 = vtk.copy() if vtk is not None else None
     return z, p, psi0
 
 
@@ -165,3 +167,33 @@ def test_exact_powers_match_reference_gpu_run(name, tmp_path):
     assert seen >= 2
     assert rel_l2(staged, z["psi_final"]) <= 1e-10
     assert rel_l2(fused, z["psi_final"]) <= 1e-10
+
+
+# The reference's own 2-D benchmark size (4096^2, as many points as 256^3):
+# its triangle lattice with a Gaussian seed (initialize.cu:95-197, eps 0.1,
+# dt 0.25), 101 iterations on the double-precision-power build; the fixture
+# keeps every 16th point of the final field in each direction.
+def test_exact_powers_match_reference_at_4096(tmp_path):
+    import xpfc_cuda_gb300 as X
+    z, p, psi0 = _case(X, "xp_tri4096_t25", tmp_path)
+    p.ref_compat = 0
+    st = int(z["sample_stride"][0])
+
+    def sample(f):
+        return f.reshape(p.Mx, p.My)[::st, ::st]
+
+    with X.Xpfc(p) as x:
+        x.initialize(psi0)
+        recs = x.step(p.nsteps)
+        fused = sample(x.copy2cpu())
+    with X.Xpfc(p) as x:
+        x.initialize(psi0)
+        F, _ = X.run_reference_loop(x, p.nsteps, p.t_sample)
+        staged = sample(x.download(X._lib.BUF_PSI_NP1_R))
+    got = {r["iteration"]: r["F"] for r in recs if r["F"] is not None}
+    assert len(z["F"]) >= 6
+    for it, v in z["F"]:
+        assert abs(F[int(it)] - v) <= 1e-12 * abs(v), ("staged", it, F[int(it)], v)
+        assert abs(got[int(it)] - v) <= 1e-12 * abs(v), ("fused", it, got[int(it)], v)
+    assert rel_l2(staged.reshape(-1), z["psi_sample"].reshape(-1)) <= 1e-10
+    assert rel_l2(fused.reshape(-1), z["psi_sample"].reshape(-1)) <= 1e-10

@@ -265,7 +265,7 @@ static void par_chunks(size_t n, F fn) {
 // difference is added to every value when the mean is not psi0).  The 16
 // chunks run on their own threads, or one after another when the caller
 // stages several fields in parallel (the same sums either way).
-static void stage_and_pin(double *dst, const double *src, size_t n, double psi0, bool threaded = true) {
+static void stage_and_pin_chunks(double *dst, const double *src, size_t n, double psi0, bool threaded) {
     double part[16] = {0.0};
     auto sum_chunk = [&](int k, size_t b, size_t e) {
         double s = 0.0;
@@ -293,6 +293,23 @@ static void stage_and_pin(double *dst, const double *src, size_t n, double psi0,
     } else {
         for (int k = 0; k < 16; k++) add_chunk(k, n * k / 16, n * (k + 1) / 16);
     }
+}
+
+// A solve in the reference's semantics (ic_kind XPFC_IC_REFERENCE: a
+// pfc.input deck) pins its mean exactly as configure_avg_density does: one
+// sum in index order from 0.0 (Avg_calc.cu:3-19).  The order matters on large
+// fields that are nearly constant: over 16.7M values of about 0.05 the
+// rounding of a running sum is systematic, and a sum in 16 chunks differs
+// from the reference's by about 1e-10 of the mean, which shifts the free
+// energy by about 5e-10 (measured on 4096^2).  Other solves take the chunked
+// sum on host threads.
+static void stage_and_pin(double *dst, const double *src, size_t n, const xpfc_params &p, bool threaded = true) {
+    if (p.ic_kind == XPFC_IC_REFERENCE) {
+        memcpy(dst, src, sizeof(double) * n);
+        pin_mean(dst, n, p.psi0);
+        return;
+    }
+    stage_and_pin_chunks(dst, src, n, p.psi0, threaded);
 }
 
 // Pinned host staging for the synchronous initial-field uploads
@@ -908,7 +925,11 @@ static int init_fused(xpfc_ctx *ctx, const double *dpsi) {
 // ---------------------------------------------------------------------------
 // initial fields on the device (every generator but the VTK restart)
 // ---------------------------------------------------------------------------
-static bool ic_on_device(const xpfc_params &p) { return !(p.ic_kind == XPFC_IC_REFERENCE && p.iconfig == 10); }
+// The reference's own initial conditions (its lattices, seeds and the VTK
+// restart) are built on the host by the restatement of initialize.cu, whose
+// mean pin keeps the reference's summation order (see stage_and_pin); the
+// library's generators (noise liquid, fcc seed) run on the device.
+static bool ic_on_device(const xpfc_params &p) { return p.ic_kind != XPFC_IC_REFERENCE; }
 
 // Enqueues p's initial field (mean pinned to psi0) into dpsi on stream s;
 // scratch: IC_SCRATCH device doubles.  Returns a status and sets *why.
@@ -1001,9 +1022,9 @@ extern "C" int xpfc_initialize(xpfc_ctx *ctx, const double *host_psi) {
         double *h = (double *)upload_pool(sizeof(double) * n);
         if (!h) return fail(ctx, XPFC_ENOMEM, "pinned upload staging");
         if (host_psi) {
-            stage_and_pin(h, host_psi, n, ctx->p.psi0);   // configure_avg_density, Avg_calc.cu:21-43
+            stage_and_pin(h, host_psi, n, ctx->p);   // configure_avg_density, Avg_calc.cu:21-43
         } else {
-            rc = build_initial_field(&ctx->p, h);   // the VTK restart
+            rc = build_initial_field(&ctx->p, h);   // the reference's initial conditions
             if (rc != XPFC_OK) return fail(ctx, rc, thread_error());
         }
         XPFC_CUDA(ctx, cudaMemcpyAsync(dpsi, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -2146,13 +2167,13 @@ static int init_group(xpfc_ctx *ctx, const std::vector<const double *> &fields, 
         }
     }
     if (given.size() == 1) {
-        stage_and_pin(h + given[0] * n, fields[given[0]], n, ctx->inst[given[0]].psi0);
+        stage_and_pin(h + given[0] * n, fields[given[0]], n, ctx->inst[given[0]]);
     } else if (!given.empty()) {
         std::atomic<size_t> next{0};
         auto work = [&] {
             for (size_t i; (i = next.fetch_add(1)) < given.size();) {
                 const size_t k = given[i];
-                stage_and_pin(h + k * n, fields[k], n, ctx->inst[k].psi0, false);
+                stage_and_pin(h + k * n, fields[k], n, ctx->inst[k], false);
             }
         };
         std::vector<std::thread> th;
