@@ -19,6 +19,7 @@ reference loop (its TIMING line, main.cu:305,437) at 512^2 and 4096^2.
 Usage (GPU machine, sources staged):
     python tests/golden/make_golden_gpu.py [--out DIR] [--no-timing]
     python tests/golden/make_golden_gpu.py --exact-powers [--out DIR]
+    python tests/golden/make_golden_gpu.py --float-4096 [--out DIR]
 """
 import argparse
 import json
@@ -135,18 +136,43 @@ def exact_powers(progs, info, out, only=None):
         print("xp", name, "F", xp["F"][:2], "...", xp["F"][-1:], "timing", xp["timing"], flush=True)
 
 
+def float_4096(progs, info, out):
+    """The 4096^2 deck on the full-precision-output build in the reference's
+    own semantics (float powers): gpu_tri4096_t25.npz."""
+    name, text = TRI4096
+    hp = ref_gpu.run(progs["xpfc_ref_hp"], text, t_sample_of(text), timeout=1800)
+    if hp["returncode"] != 0 or "psi_final" not in hp:
+        print(name, "FAILED", hp["returncode"], hp["stdout_tail"][-1500:], hp["stderr_tail"][-1500:], flush=True)
+        return
+    nx, ny = hp["dims"][0], hp["dims"][1]
+    np.savez_compressed(
+        os.path.join(out, "gpu_%s.npz" % name),
+        deck=np.frombuffer(text.encode(), dtype=np.uint8),
+        F=np.array(hp["F"], dtype=np.float64).reshape(-1, 2),
+        RMS=np.array(hp["RMS"], dtype=np.float64).reshape(-1, 2),
+        final_iteration=np.array([hp["final_iteration"]]),
+        psi_sample=hp["psi_final"].reshape(nx, ny)[::SAMPLE, ::SAMPLE].copy(),
+        sample_stride=np.array([SAMPLE]),
+        meta=np.frombuffer(json.dumps(dict(info, timing=hp["timing"])).encode(), dtype=np.uint8))
+    print(name, "F", hp["F"][:2], "...", hp["F"][-1:], "timing", hp["timing"], flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--no-timing", action="store_true")
     ap.add_argument("--only", default=None, help="comma-separated deck names")
     ap.add_argument("--exact-powers", action="store_true")
+    ap.add_argument("--float-4096", action="store_true", help="the 4096^2 deck in the reference's float powers")
     a = ap.parse_args()
     os.makedirs(a.out, exist_ok=True)
     progs = ref_gpu.build()
     info = meta()
     if a.exact_powers:
         exact_powers(progs, info, a.out, a.only)
+        return
+    if a.float_4096:
+        float_4096(progs, info, a.out)
         return
 
     # the program linked against cuFFT as shipped, on the smallest deck
