@@ -20,8 +20,8 @@ Three more legs ride on the same line: "sweep" (64 independent solves of
 1000 steps through one xpfc_batch: solves/s, against the same solves one
 context at a time), "serve" (a Poisson stream of solve requests through
 xpfc_server: latency percentiles and served grid-point-steps/s, every solve
-in a context of its own, then with merged groups, and a stream of 64^3
-requests both ways) and "two_d"
+in a context of its own, then with merged groups, and a saturating burst
+of 64^3 requests both ways) and "two_d"
 (the 2-D step at 4096^2, the reference's own benchmark size, both
 precisions).
 
@@ -384,14 +384,15 @@ def run_serve(args, rank, local, group, barrier):
         m["merge_max"] = args.serve_merge
         out["with_merging"] = m
         same &= m["same_as_alone"]
-        # a stream of 64^3 requests alone (passes bound by launch latency),
-        # without and with merging
-        srate = 100.0
+        # a burst of 64^3 requests (passes bound by launch latency) that
+        # saturates the server, without and with merging: its capacity
+        srate = 1000.0
         small = SV.request_stream(200, rate=srate, seed=100 + rank, sizes=(64,), weights=(1.0,), device=local)
         s0 = brief(*play(small, 0), srate)
         s1 = brief(*play(small, args.serve_merge), srate)
-        out["small_grid_stream"] = {"workload": "200 requests of 64^3, Poisson 100/s, steps U[200,5000], "
-                                                "sweep physics", "without_merging": s0, "with_merging": s1,
+        out["small_grid_stream"] = {"workload": "200 requests of 64^3, Poisson 1000/s (a burst that saturates the "
+                                                "server), steps U[200,5000], sweep physics",
+                                    "without_merging": s0, "with_merging": s1,
                                     "solves_per_s_ratio": s1["solves_per_s"] / s0["solves_per_s"]}
     if not args.no_serve_seq:
         # the plain sequential baselines: the same requests one at a time, each

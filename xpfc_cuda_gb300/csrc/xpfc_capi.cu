@@ -1343,10 +1343,15 @@ static bool autotune_on() {
     return on;
 }
 
+// Chunk counts above one are candidates only for states of at least 32 MB
+// (the threshold of the default): a smaller state stays in L2 through the
+// xy passes whole, and timing candidates of a small grid amid other solves'
+// work (a server) could remember a many-launch schedule for its shape.
 static std::vector<Sched> sched_candidates(xpfc_ctx *ctx) {
     std::vector<Sched> out;
     std::vector<int> chunks = {1};
-    if (!getenv("XPFC_XY_CHUNKS") && ensure_aux(ctx))
+    const size_t slab = ctx->esz * (size_t)ctx->ncells * ctx->nb;
+    if (!getenv("XPFC_XY_CHUNKS") && slab >= ((size_t)32 << 20) && ensure_aux(ctx))
         for (int c : {2, 4, 8})
             if (ctx->n2 % c == 0 && ctx->n2 / c >= 8) chunks.push_back(c);
     for (int c : chunks) out.push_back({c, ctx->use_tma});
@@ -1376,7 +1381,7 @@ static int plain_step(xpfc_ctx *ctx, long long i) {
 // shape, or the defaults.  Returns true when the context still has to tune.
 static bool sched_init(xpfc_ctx *ctx) {
     if (ctx->tuned) return false;
-    if (!ctx->three_d || !autotune_on() || ctx->profiling) {
+    if (!ctx->three_d || !autotune_on() || ctx->profiling || sched_candidates(ctx).size() < 2) {
         ctx->tuned = true;
         return false;
     }
