@@ -200,8 +200,8 @@ def test_server_merged_group_keeps_failures_local():
 
 def test_server_merged_group_context_reused():
     """A finished merged group's context goes to the pool; the next group of
-    the same grid and size takes it with new params (tables, pinned means,
-    seeds) and still gives every solve's results alone."""
+    the same grid and size takes it with new params (box, tables, pinned
+    means, seeds) and still gives every solve's results alone."""
     import xpfc_cuda_gb300 as X
     M, D = X._lib.MIXED, X._lib.FP64
     blocker = _params(X, 128, D, 0.05, 0.25, SINGLE_PEAK, 0.0, 99)
@@ -209,6 +209,10 @@ def test_server_merged_group_context_reused():
               (_params(X, 32, M, 0.05, 0.25, SINGLE_PEAK, 0.01, 32), 27)],
              [(_params(X, 32, M, 0.02, 0.3, SINGLE_PEAK, 0.01, 33), 26),
               (_params(X, 32, M, 0.06, 0.28, FCC_PEAKS, 0.01, 34), 31)]]
+    # the second wave's box differs (dx 0.15): the pooled context keys on the
+    # grid, so it must take the new box's k-grid
+    for p, _ in waves[1]:
+        X.set_params(p, Lx=32 * 0.15, Ly=32 * 0.15, Lz=32 * 0.15, ff_factor=0.15 ** 3)
     # one context in flight (a merged group counts once): each wave queues
     # behind its blocker and forms its group when the blocker finishes
     with X.Server(max_running=1, chunk_steps=5, merge_max=8) as s:
